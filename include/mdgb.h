@@ -1,0 +1,230 @@
+/*
+ * mdgb.h -- C ABI of the GB300 molecular-dynamics step engine (libmdgb.so).
+ *
+ * Drop-in boundary for moldyn's force / neighbour / integration path.  The
+ * reference (a Rust workspace) has no FFI of its own; its boundary is the
+ * solver crate's Rust API, which these entry points replace one for one:
+ *
+ *   mdgb_set_potential        Potential::new_lennard_jones + PotentialsDatabase::set_potential
+ *                             (solver/src/solver/potential.rs:27-55, :141-144)
+ *   mdgb_set_potential_raw    PotentialsDatabase::load_potentials_from_file entries
+ *                             (potential.rs:125-139: sigma, eps, r_cut, u_cut as stored)
+ *   mdgb_upload_state         State / StateToSave -> device (core/src/particle.rs:27-32,
+ *                             core/src/save_data.rs:129-151)
+ *   mdgb_compute_forces       update_force(&PotentialsDatabase, &mut State)
+ *                             (solver/src/solver/potential.rs:158-216)
+ *   mdgb_step                 Integrator::VerletMethod.calculate(..) called nsteps times with
+ *                             Option<(&mut Barostat, P0)>, Option<(&mut Thermostat, T0)>
+ *                             (solver/src/solver/integrator.rs:14-59,
+ *                              solver/src/initializer/thermostat.rs:24-72,
+ *                              solver/src/initializer/barostat.rs:21-56)
+ *   mdgb_download_state       device -> State (positions, velocities, force, potential, temp, box)
+ *   mdgb_macro_parameters     get_center_of_mass_velocity, get_momentum_of_system,
+ *                             get_kinetic_energy, get_thermal_energy, get_potential_energy,
+ *                             get_pressure, get_temperature
+ *                             (solver/src/macro_parameters/{mod,energy,pressure,temperature}.rs)
+ *   mdgb_ensemble_*           no single counterpart: many independent States, each driven as
+ *                             `solve` drives one (cli/src/commands.rs:82-191)
+ *   mdgb_lj_new / mdgb_lj_eval   Potential::new_lennard_jones / get_potential_and_force
+ *                             (potential.rs:27-75), host only
+ *   mdgb_lattice              initialize_particles_position (solver/src/initializer/position.rs:
+ *                             25-99, :155-174), host only
+ *   mdgb_maxwell_boltzmann    initialize_velocities_maxwell_boltzmann
+ *                             (solver/src/initializer/velocity.rs:6-29), host only, seeded
+ *
+ * Conventions: every call returns an int status (MDGB_OK == 0); no C++
+ * exception crosses the ABI; mdgb_last_error() gives the message of the last
+ * failure on a handle.  One handle per host thread: calls on a handle are not
+ * thread-safe.  All device work of a handle runs on one CUDA stream owned by
+ * the handle.  Host arrays passed in are copied; the caller keeps ownership.
+ *
+ * Atom order: atoms are passed as one flat array with a type id per atom.
+ * The reference groups atoms by type (`Vec<Vec<Particle>>`); the k-th atom of
+ * type t in the flat array is the reference's particles[t][k].  Every array
+ * returned by the engine is in the caller's original flat order.
+ *
+ * Units are the reference's (nm, 1e-27 kg, 1e-21 J, ps, K for temperature,
+ * MPa for pressure); the engine applies the reference's formulas literally,
+ * so reduced LJ units work with sigma = eps = mass = 1 and temperatures given
+ * as T* * 100 / K_B.
+ */
+#ifndef MDGB_H
+#define MDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define MDGB_API __declspec(dllexport)
+#else
+#define MDGB_API __attribute__((visibility("default")))
+#endif
+
+#define MDGB_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------- */
+#define MDGB_OK 0
+#define MDGB_ERR_INVALID_ARGUMENT 1
+#define MDGB_ERR_CUDA 2
+#define MDGB_ERR_NO_STATE 3
+#define MDGB_ERR_NEIGHBOR_OVERFLOW 4   /* list capacity exceeded and regrowth failed */
+#define MDGB_ERR_FIXED_POINT_OVERFLOW 5 /* a force sum left the 64-bit fixed-point range */
+#define MDGB_ERR_UNSUPPORTED 6
+#define MDGB_ERR_DEVICE_TIMEOUT 7      /* a bounded device-side wait gave up */
+#define MDGB_ERR_OUT_OF_MEMORY 8
+#define MDGB_ERR_SKIN_VIOLATION 9      /* fixed rebuild interval too long for the motion */
+
+/* ---- precision ------------------------------------------------------- */
+#define MDGB_PRECISION_FP64 0  /* plain path: the reference's FP64 arithmetic */
+#define MDGB_PRECISION_MIXED 1 /* FP32 pair maths, 64-bit fixed-point force sums, FP64 drift/reductions */
+
+/* ---- flags ----------------------------------------------------------- */
+/* FP64 only: reproduce the reference's summation order (neighbour lists in
+ * atom order, serial thermostat/barostat/macro reductions) so forces and
+ * trajectories are bit-identical to the reference's FP64 CPU results. */
+#define MDGB_FLAG_REFERENCE_ORDER 1u
+/* Record CUDA events around every kernel launch (per-kernel timing). */
+#define MDGB_FLAG_PROFILE 2u
+/* Drive the per-step force pass with the persistent work-queue kernel. */
+#define MDGB_FLAG_PERSISTENT 4u
+
+typedef struct mdgb_engine mdgb_engine;
+
+typedef struct {
+    int precision;          /* MDGB_PRECISION_* */
+    double skin;            /* Verlet skin (length); <= 0: 0.12 * largest r_cut (= 0.3 sigma) */
+    int rebuild_every;      /* 0: rebuild when displacement needs it; >0: fixed interval, checked */
+    int threads_per_atom;   /* 0: autotune; else 1, 2, 4 or 8 */
+    int graph_steps;        /* >1: capture that many steps into one CUDA graph launch */
+    int neighbor_capacity;  /* 0: automatic (grows on overflow) */
+    int device;             /* CUDA device ordinal */
+    unsigned flags;         /* MDGB_FLAG_* */
+} mdgb_config;
+
+/* Thermostat (solver/src/initializer/thermostat.rs:4-20).  lambda and psi
+ * are updated in place by mdgb_step, as the reference mutates its enum. */
+#define MDGB_THERMOSTAT_BERENDSEN 0
+#define MDGB_THERMOSTAT_NOSE_HOOVER 1
+typedef struct {
+    int kind;
+    double tau;
+    double target_temperature;  /* T0 passed beside the thermostat (K) */
+    double lambda;
+    double psi;
+} mdgb_thermostat;
+
+/* Barostat::Berendsen (solver/src/initializer/barostat.rs:4-16); myu in/out. */
+typedef struct {
+    double beta;
+    double tau;
+    double target_pressure;     /* P0 passed beside the barostat */
+    double myu;
+} mdgb_barostat;
+
+/* Macro parameters of one particle type (solver/src/macro_parameters). */
+typedef struct {
+    double kinetic_energy;      /* get_kinetic_energy */
+    double potential_energy;    /* get_potential_energy (sum of potential / 2) */
+    double thermal_energy;      /* get_thermal_energy with the COM velocity */
+    double temperature;         /* get_temperature(thermal_energy, count of this type) */
+    double pressure;            /* get_pressure */
+    double com_velocity[3];     /* get_center_of_mass_velocity */
+    double momentum[3];         /* get_momentum_of_system */
+    int64_t count;
+} mdgb_macro;
+
+/* Engine counters (host-side view, filled by mdgb_get_stats). */
+typedef struct {
+    int64_t steps;              /* integrator steps taken */
+    int64_t rebuilds;           /* neighbour-list rebuilds (sum over replicas) */
+    int64_t kernel_launches;    /* kernels launched by this handle */
+    int64_t graph_launches;
+    int neighbor_capacity;
+    int max_neighbors;          /* largest list seen at the last rebuild */
+    int threads_per_atom;
+    int retries;                /* chunks re-run after an overflow */
+    double force_ms;            /* with MDGB_FLAG_PROFILE: summed force-kernel time */
+    int64_t force_launches;
+    double integrate_ms;        /* summed integrate/rebuild-kernel time */
+    int64_t integrate_launches;
+} mdgb_stats;
+
+/* ---- lifecycle ------------------------------------------------------- */
+MDGB_API int mdgb_abi_version(void);
+MDGB_API int mdgb_config_default(mdgb_config* cfg);
+MDGB_API int mdgb_create(const mdgb_config* cfg, mdgb_engine** out);
+MDGB_API int mdgb_destroy(mdgb_engine* e);
+MDGB_API const char* mdgb_last_error(const mdgb_engine* e);
+MDGB_API const char* mdgb_status_string(int status);
+/* The CUDA stream (cudaStream_t) all work of the handle runs on. */
+MDGB_API void* mdgb_stream(mdgb_engine* e);
+
+/* ---- potentials ------------------------------------------------------ */
+MDGB_API int mdgb_set_potential(mdgb_engine* e, uint16_t t0, uint16_t t1, double sigma, double eps);
+MDGB_API int mdgb_set_potential_raw(mdgb_engine* e, uint16_t t0, uint16_t t1, double sigma,
+                                    double eps, double r_cut, double u_cut);
+
+/* ---- single system --------------------------------------------------- */
+MDGB_API int mdgb_upload_state(mdgb_engine* e, int64_t n, const uint16_t* type, const double* pos,
+                               const double* vel, const double* mass_per_type, int ntypes,
+                               const double box[3]);
+/* The reference's Particle carries force, potential and temp into the next
+ * Integrator::calculate; upload them (caller order; any pointer may be NULL)
+ * after mdgb_upload_state to resume exactly. */
+MDGB_API int mdgb_upload_forces(mdgb_engine* e, const double* force, const double* potential,
+                                const double* temp);
+MDGB_API int mdgb_compute_forces(mdgb_engine* e);
+MDGB_API int mdgb_step(mdgb_engine* e, int64_t nsteps, double dt, mdgb_thermostat* thermostat,
+                       mdgb_barostat* barostat);
+MDGB_API int mdgb_download_state(mdgb_engine* e, double* pos, double* vel, double* force,
+                                 double* potential, double* temp, double box[3]);
+MDGB_API int mdgb_macro_parameters(mdgb_engine* e, int type, mdgb_macro* out);
+
+/* ---- ensembles of independent replicas ------------------------------ */
+/* offsets[nrep+1]: replica r owns flat atoms [offsets[r], offsets[r+1]).
+ * boxes[3*nrep].  Each replica is its own State; the type table is shared. */
+MDGB_API int mdgb_ensemble_upload(mdgb_engine* e, int nrep, const int64_t* offsets,
+                                  const uint16_t* type, const double* pos, const double* vel,
+                                  const double* mass_per_type, int ntypes, const double* boxes);
+/* Per-replica coupling; either array may be NULL (no coupling of that kind). */
+MDGB_API int mdgb_ensemble_set_coupling(mdgb_engine* e, const mdgb_thermostat* thermostats,
+                                        const mdgb_barostat* barostats);
+MDGB_API int mdgb_ensemble_step(mdgb_engine* e, int64_t nsteps, double dt);
+MDGB_API int mdgb_ensemble_get_coupling(mdgb_engine* e, mdgb_thermostat* thermostats,
+                                        mdgb_barostat* barostats);
+MDGB_API int mdgb_ensemble_download(mdgb_engine* e, double* pos, double* vel, double* force,
+                                    double* potential, double* temp, double* boxes);
+MDGB_API int mdgb_ensemble_macro(mdgb_engine* e, int type, mdgb_macro* out_per_replica);
+
+/* ---- diagnostics ----------------------------------------------------- */
+/* The set of interacting pairs of the last force evaluation: every (i, j),
+ * caller indices, whose distance by the reference's FP64 rule is <= r_cut
+ * (the pairs update_force sums, potential.rs:176-204), read from the
+ * neighbour list.  Writes up to `capacity` pairs; *count receives the total. */
+MDGB_API int mdgb_interacting_pairs(mdgb_engine* e, int64_t capacity, int32_t* out_i, int32_t* out_j,
+                                    int64_t* count);
+MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out);
+MDGB_API int mdgb_reset_stats(mdgb_engine* e);
+MDGB_API int mdgb_synchronize(mdgb_engine* e);
+
+/* ---- host-only helpers (no GPU) ------------------------------------- */
+/* out = {sigma, eps, r_cut, u_cut} */
+MDGB_API int mdgb_lj_new(double sigma, double eps, double out[4]);
+MDGB_API int mdgb_lj_eval(const double pot[4], double r, double* u, double* dudr);
+/* kind 0 = U (simple cubic), 1 = FCC; out has 3*n doubles, n = nx*ny*nz*(1 or 4) */
+MDGB_API int mdgb_lattice(int kind, int64_t nx, int64_t ny, int64_t nz, double a,
+                          const double start[3], double* out);
+/* Maxwell-Boltzmann at temperature T (K) for mass m, seeded and portable:
+ * sigma_v = sqrt(K_B * T * 0.01 / m); the first n/2 atoms get +v, the next
+ * n/2 get -v (zero momentum); with odd n the last atom keeps v = 0. */
+MDGB_API int mdgb_maxwell_boltzmann(int64_t n, double temperature, double mass, uint64_t seed,
+                                    double* out_vel);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MDGB_H */

@@ -1,0 +1,289 @@
+// kernels_force.cu -- Lennard-Jones pair forces over the Verlet list.
+//
+// Replaces update_force (solver/src/solver/potential.rs:158-216): per atom i
+// the force F_i = sum_j r_ij/|r_ij| * dU/dr(|r_ij|), the potential sum
+// U_i = sum_j U(|r_ij|) and temp_i = sum_j F_ij . r_ij over every j with
+// |r_ij| <= r_cut, r_ij = x_j - x_i taken to the image picked by the
+// reference's single-shift rule (potential.rs:186-200).
+//
+// k_force_fp64  -- the plain path.  Every pair is evaluated with the
+//   reference's FP64 operation sequence through explicit round-to-nearest
+//   intrinsics (no contraction), so each pair term carries the reference's
+//   bits; with MDGB_FLAG_REFERENCE_ORDER the list is in the reference's j
+//   order and the per-atom sums are bit-identical too.  An FP32 prefilter on
+//   the mirror skips candidates that are certainly outside r_cut.
+// k_force_mixed -- the chosen path.  FP32 pair maths from the float4 mirror
+//   (cell-relative coordinates, periodic cell shift from the list entry),
+//   force sums in deterministic 64-bit fixed point, potential/virial in FP32
+//   per atom (FP64 across atoms).  Pairs whose FP32 r^2 lies within 1e-5 of
+//   r_cut^2 are re-decided with the reference's FP64 arithmetic, so the set
+//   of interacting pairs equals the reference's.
+//
+// Both end with the second half kick v += F dt/2m (integrator.rs:49-55) when
+// called from a step.  TPA threads share one atom's list; their partial sums
+// are combined by a fixed shuffle tree.
+#include "mdgb_internal.cuh"
+
+namespace mdgb {
+
+__device__ __forceinline__ void shift_table(float4* tab, const RepDev* R) {
+    if (threadIdx.x < 27) {
+        const int c = threadIdx.x;
+        const float dx = (float)(c % 3 - 1), dy = (float)((c / 3) % 3 - 1), dz = (float)(c / 9 - 1);
+        tab[c] = make_float4(dx * (float)R->cs[0], dy * (float)R->cs[1], dz * (float)R->cs[2], 0.f);
+    }
+}
+
+// The reference's FP64 displacement and distance (potential.rs:181-201).
+__device__ __forceinline__ double ref_distance(const double4 pi, const double4 pj, const double* box,
+                                               double& rx, double& ry, double& rz) {
+    rx = __dsub_rn(pj.x, pi.x);
+    ry = __dsub_rn(pj.y, pi.y);
+    rz = __dsub_rn(pj.z, pi.z);
+    const double hx = 0.5 * box[0], hy = 0.5 * box[1], hz = 0.5 * box[2];
+    if (rx < -hx) rx = __dadd_rn(rx, box[0]); else if (rx > hx) rx = __dsub_rn(rx, box[0]);
+    if (ry < -hy) ry = __dadd_rn(ry, box[1]); else if (ry > hy) ry = __dsub_rn(ry, box[1]);
+    if (rz < -hz) rz = __dadd_rn(rz, box[2]); else if (rz > hz) rz = __dsub_rn(rz, box[2]);
+    const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+    return __dsqrt_rn(r2);
+}
+
+template <int TPA>
+__device__ __forceinline__ long long tpa_sum_ll(long long v) {
+#pragma unroll
+    for (int off = TPA / 2; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off, TPA);
+    return v;
+}
+template <int TPA>
+__device__ __forceinline__ double tpa_sum_d(double v) {
+#pragma unroll
+    for (int off = TPA / 2; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off, TPA);
+    return v;
+}
+template <int TPA>
+__device__ __forceinline__ float tpa_sum_f(float v) {
+#pragma unroll
+    for (int off = TPA / 2; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off, TPA);
+    return v;
+}
+
+__device__ __forceinline__ int next_tile(const Dev& d, bool persistent, int& iter, int* s_tile) {
+    if (!persistent) return (iter++ == 0) ? (int)blockIdx.x : -1;
+    __syncthreads();
+    if (threadIdx.x == 0) *s_tile = (int)atomicAdd(d.queue, 1u);
+    __syncthreads();
+    const int q = *s_tile;
+    if (q >= d.ntiles) return -1;
+    return d.tile_order[q];
+}
+
+// ---------------------------------------------------------------------------
+template <int TPA, bool KICK, bool PERSIST>
+__global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp) {
+    __shared__ float4 tab[27];
+    __shared__ int s_tile;
+    const int N = d.ntot;
+    const int a = threadIdx.x / TPA, lane = threadIdx.x % TPA;
+    int iter = 0;
+    for (;;) {
+        const int t = next_tile(d, PERSIST, iter, &s_tile);
+        if (t < 0) return;
+        const int4 tl = d.tiles[t];
+        const RepDev* R = d.rep + tl.x;
+        __syncthreads();
+        shift_table(tab, R);
+        __syncthreads();
+        const double box[3] = {R->box[0], R->box[1], R->box[2]};
+        const float Lf[3] = {(float)box[0], (float)box[1], (float)box[2]};
+        const bool brute = R->mode == MODE_BRUTE;
+        const int s = tl.y + a;
+        const bool act = a < tl.z;
+        double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0, vr = 0.0;
+        int ty = 0;
+        if (act) {
+            const double4 pi = d.pos[s];
+            const float4 mi = d.mir[s];
+            ty = type_of(pi);
+            const int n = d.nn[s];
+            for (int k = lane; k < n; k += TPA) {
+                const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                const int j = (int)(e & IDX_MASK);
+                const PairDev& P = d.pair[ty * MAX_TYPES + type_of(__ldg(d.mir + j))];
+                // FP32 prefilter (certainly outside r_cut -> skip)
+                {
+                    const float4 mj = __ldg(d.mir + j);
+                    const float4 sh = tab[e >> IDX_BITS];
+                    float ex = mj.x - mi.x + sh.x, ey = mj.y - mi.y + sh.y, ez = mj.z - mi.z + sh.z;
+                    if (brute) {
+                        if (ex < -0.5f * Lf[0]) ex += Lf[0]; else if (ex > 0.5f * Lf[0]) ex -= Lf[0];
+                        if (ey < -0.5f * Lf[1]) ey += Lf[1]; else if (ey > 0.5f * Lf[1]) ey -= Lf[1];
+                        if (ez < -0.5f * Lf[2]) ez += Lf[2]; else if (ez > 0.5f * Lf[2]) ez -= Lf[2];
+                    }
+                    if (ex * ex + ey * ey + ez * ez > P.rc2f_hi * 1.0001f) continue;
+                }
+                const double4 pj = d.pos[j];
+                double rx, ry, rz;
+                const double r = ref_distance(pi, pj, box, rx, ry, rz);
+                if (r > P.rc) continue;                                          // :202-204
+                // potential.rs:57-75 get_potential_and_force
+                const double sr = __ddiv_rn(P.sigma, r);
+                const double s2 = __dmul_rn(sr, sr);
+                const double s4 = __dmul_rn(s2, s2);
+                const double s6 = __dmul_rn(s2, s4);
+                const double s12 = __dmul_rn(s6, s6);
+                const double u = __dsub_rn(__dmul_rn(P.eps4, __dsub_rn(s12, s6)), P.ucut);
+                const double dudr = __dmul_rn(__ddiv_rn(P.eps24, r), __dsub_rn(s6, __dmul_rn(2.0, s12)));
+                // :207-211
+                const double gx = __dmul_rn(__ddiv_rn(rx, r), dudr);
+                const double gy = __dmul_rn(__ddiv_rn(ry, r), dudr);
+                const double gz = __dmul_rn(__ddiv_rn(rz, r), dudr);
+                const double tt = __dadd_rn(__dadd_rn(__dmul_rn(gx, rx), __dmul_rn(gy, ry)), __dmul_rn(gz, rz));
+                fx = __dadd_rn(fx, gx); fy = __dadd_rn(fy, gy); fz = __dadd_rn(fz, gz);
+                pe = __dadd_rn(pe, u);
+                vr = __dadd_rn(vr, tt);
+            }
+        }
+        if (TPA > 1) {
+            fx = tpa_sum_d<TPA>(fx); fy = tpa_sum_d<TPA>(fy); fz = tpa_sum_d<TPA>(fz);
+            pe = tpa_sum_d<TPA>(pe); vr = tpa_sum_d<TPA>(vr);
+        }
+        if (act && lane == 0) {
+            d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
+            d.epot[s] = pe; d.evir[s] = vr;
+            if (KICK) {                                                          // integrator.rs:49-55
+                const double c = sp.kick_c[ty];
+                d.vel[s] = __dadd_rn(d.vel[s], __dmul_rn(fx, c));
+                d.vel[N + s] = __dadd_rn(d.vel[N + s], __dmul_rn(fy, c));
+                d.vel[2 * N + s] = __dadd_rn(d.vel[2 * N + s], __dmul_rn(fz, c));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <int TPA, bool SINGLE, bool KICK, bool PERSIST>
+__global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp) {
+    __shared__ float4 tab[27];
+    __shared__ int s_tile;
+    const int N = d.ntot;
+    const int a = threadIdx.x / TPA, lane = threadIdx.x % TPA;
+    const float fscale = d.fscale;
+    // |dx * fs * fscale| stays below 2^55 for every term, so 256 terms cannot overflow.
+    const float term_limit = 36028797018963968.0f / (float)(d.rlist * 1.01);
+    int iter = 0;
+    for (;;) {
+        const int t = next_tile(d, PERSIST, iter, &s_tile);
+        if (t < 0) return;
+        const int4 tl = d.tiles[t];
+        const RepDev* R = d.rep + tl.x;
+        __syncthreads();
+        shift_table(tab, R);
+        __syncthreads();
+        const bool brute = R->mode == MODE_BRUTE;
+        const float Lf[3] = {(float)R->box[0], (float)R->box[1], (float)R->box[2]};
+        const int s = tl.y + a;
+        const bool act = a < tl.z;
+        long long ax = 0, ay = 0, az = 0;
+        float pe = 0.f, vr = 0.f, fsmax = 0.f;
+        int ty = 0;
+        if (act) {
+            const float4 xi = d.mir[s];
+            ty = type_of(xi);
+            PairDev P0;
+            if (SINGLE) P0 = d.pair[ty * MAX_TYPES + ty];
+            const int n = d.nn[s];
+            for (int k = lane; k < n; k += TPA) {
+                const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                const int j = (int)(e & IDX_MASK);
+                const float4 xj = __ldg(d.mir + j);
+                const float4 sh = tab[e >> IDX_BITS];
+                float dx = xj.x - xi.x + sh.x, dy = xj.y - xi.y + sh.y, dz = xj.z - xi.z + sh.z;
+                bool near_half = false;
+                if (brute) {
+                    if (dx < -0.5f * Lf[0]) dx += Lf[0]; else if (dx > 0.5f * Lf[0]) dx -= Lf[0];
+                    if (dy < -0.5f * Lf[1]) dy += Lf[1]; else if (dy > 0.5f * Lf[1]) dy -= Lf[1];
+                    if (dz < -0.5f * Lf[2]) dz += Lf[2]; else if (dz > 0.5f * Lf[2]) dz -= Lf[2];
+                    near_half = fabsf(fabsf(dx) - 0.5f * Lf[0]) < 1e-5f * Lf[0] ||
+                                fabsf(fabsf(dy) - 0.5f * Lf[1]) < 1e-5f * Lf[1] ||
+                                fabsf(fabsf(dz) - 0.5f * Lf[2]) < 1e-5f * Lf[2];
+                }
+                const PairDev& P = SINGLE ? P0 : d.pair[ty * MAX_TYPES + type_of(xj)];
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 > P.rc2f_hi && !near_half) continue;
+                if (r2 >= P.rc2f_lo || near_half) {
+                    // decide with the reference's FP64 arithmetic (potential.rs:181-204)
+                    const double box[3] = {R->box[0], R->box[1], R->box[2]};
+                    double rx, ry, rz;
+                    const double r = ref_distance(d.pos[s], d.pos[j], box, rx, ry, rz);
+                    if (r > P.rc) continue;
+                    dx = (float)rx; dy = (float)ry; dz = (float)rz;
+                }
+                const float rr2 = dx * dx + dy * dy + dz * dz;
+                const float r2i = __fdividef(1.0f, rr2);
+                const float s2 = P.sig2f * r2i;
+                const float s6 = s2 * s2 * s2;
+                // (24 eps / r^2) s6 (1 - 2 s6) = (dU/dr) / r
+                const float fs = P.eps24f * r2i * s6 * fmaf(-2.0f, s6, 1.0f);
+                pe += fmaf(P.eps4f * s6, s6 - 1.0f, -P.ucutf);
+                vr = fmaf(fs, rr2, vr);
+                const float g = fs * fscale;
+                fsmax = fmaxf(fsmax, fabsf(g));
+                ax += __float2ll_rn(dx * g);
+                ay += __float2ll_rn(dy * g);
+                az += __float2ll_rn(dz * g);
+            }
+        }
+        if (TPA > 1) {
+            ax = tpa_sum_ll<TPA>(ax); ay = tpa_sum_ll<TPA>(ay); az = tpa_sum_ll<TPA>(az);
+            pe = tpa_sum_f<TPA>(pe); vr = tpa_sum_f<TPA>(vr);
+            fsmax = fmaxf(fsmax, 0.f);
+        }
+        if (fsmax > term_limit) atomicOr(d.err, E_FIXED);
+        if (act && lane == 0) {
+            const double fx = (double)ax * d.inv_fscale, fy = (double)ay * d.inv_fscale,
+                         fz = (double)az * d.inv_fscale;
+            d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
+            d.epot[s] = (double)pe; d.evir[s] = (double)vr;
+            if (KICK) {
+                const double c = sp.kick_c[ty];
+                d.vel[s] = __dadd_rn(d.vel[s], __dmul_rn(fx, c));
+                d.vel[N + s] = __dadd_rn(d.vel[N + s], __dmul_rn(fy, c));
+                d.vel[2 * N + s] = __dadd_rn(d.vel[2 * N + s], __dmul_rn(fz, c));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launch table.
+using force_fn = void (*)(Dev, StepParams);
+
+template <int TPA, bool KICK, bool PERSIST>
+static force_fn pick_mixed(bool single) {
+    return single ? (force_fn)k_force_mixed<TPA, true, KICK, PERSIST>
+                  : (force_fn)k_force_mixed<TPA, false, KICK, PERSIST>;
+}
+
+template <int TPA, bool PERSIST>
+static force_fn pick_tpa(bool mixed, bool single, bool kick) {
+    if (mixed) return kick ? pick_mixed<TPA, true, PERSIST>(single) : pick_mixed<TPA, false, PERSIST>(single);
+    return kick ? (force_fn)k_force_fp64<TPA, true, PERSIST> : (force_fn)k_force_fp64<TPA, false, PERSIST>;
+}
+
+template <bool PERSIST>
+static force_fn pick_persist(int tpa, bool mixed, bool single, bool kick) {
+    switch (tpa) {
+        case 1: return pick_tpa<1, PERSIST>(mixed, single, kick);
+        case 2: return pick_tpa<2, PERSIST>(mixed, single, kick);
+        case 4: return pick_tpa<4, PERSIST>(mixed, single, kick);
+        case 8: return pick_tpa<8, PERSIST>(mixed, single, kick);
+        default: return nullptr;
+    }
+}
+
+force_fn force_kernel(int tpa, bool mixed, bool single, bool kick, bool persistent) {
+    return persistent ? pick_persist<true>(tpa, mixed, single, kick)
+                      : pick_persist<false>(tpa, mixed, single, kick);
+}
+
+}  // namespace mdgb

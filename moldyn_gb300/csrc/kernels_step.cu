@@ -1,0 +1,920 @@
+// kernels_step.cu -- the per-step O(N) work of the engine in one cooperative
+// persistent kernel (k_pre), plus the macro-parameter reduction kernel.
+//
+//   [coupling]  FP64 reductions -> Berendsen lambda / mu
+//               (solver/src/initializer/thermostat.rs:24-34, barostat.rs:21-31,
+//                solver/src/macro_parameters/{mod,energy,pressure,temperature}.rs)
+//   [drift]     v += F dt/2m, thermostat scale, pending barostat scale of x,
+//               x += v dt, periodic wrap, FP32 mirror, displacement
+//               (solver/src/solver/integrator.rs:30-47, core/src/particle.rs:120-141)
+//   [rebuild]   per replica, only when the displacement (or a forced rebuild)
+//               asks for it: integer counting sort of atoms into cells
+//               (count -> exclusive scan -> scatter -> canonical order inside
+//               each cell) and the Verlet neighbour list with skin.
+//
+// Phases are separated by a bounded grid barrier (the kernel is launched
+// cooperatively, so every block is resident).  A barrier that waits longer
+// than ~2 s sets E_TIMEOUT and lets the block continue; every index derived
+// from scratch data is range-checked, so a failed barrier cannot turn into
+// an out-of-bounds access.  Data produced by another block inside the same
+// launch is read with ld.global.cg (L2), never from a possibly stale L1 line.
+//
+// This file is compiled with -fmad=false: its FP64 arithmetic (kick, drift,
+// wrap, reductions, coupling factors) keeps the reference's unfused
+// multiply-then-add rounding.
+#include "mdgb_internal.cuh"
+
+namespace mdgb {
+
+constexpr long long BARRIER_LIMIT_CYCLES = 4000000000LL;
+constexpr double K_B = 1.380648528;  // core/src/lib.rs:15
+
+static_assert(sizeof(RepDev) % 8 == 0, "RepDev must be a whole number of 8-byte words");
+
+__device__ __forceinline__ RepDev load_rep(const RepDev* p) {
+    RepDev r;
+    const long long* src = reinterpret_cast<const long long*>(p);
+    long long* dst = reinterpret_cast<long long*>(&r);
+#pragma unroll 4
+    for (int i = 0; i < (int)(sizeof(RepDev) / 8); ++i) dst[i] = __ldcg(src + i);
+    return r;
+}
+
+__device__ __forceinline__ double4 ldcg4(const double4* p) {
+    const double2 a = __ldcg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldcg(reinterpret_cast<const double2*>(p) + 1);
+    return make_double4(a.x, a.y, b.x, b.y);
+}
+
+__device__ __forceinline__ void grid_barrier(const Dev& d) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* gen = d.bar + 1;
+        const unsigned int g = *gen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(d.bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(d.bar, 0u);
+            __threadfence();
+            atomicAdd(d.bar + 1, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*gen == g) {
+                __nanosleep(100);
+                if (clock64() - t0 > BARRIER_LIMIT_CYCLES) {
+                    atomicOr(d.err, E_TIMEOUT);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Deterministic block sum of NV doubles (fixed shuffle tree, fixed warp order).
+// Result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* sm) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+    }
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sm[k * 32 + w] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = sm[k * 32];
+            for (int i = 1; i < nw; ++i) s += sm[k * 32 + i];
+            v[k] = s;
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ float block_max(float v, float* sm) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, off));
+    __syncthreads();
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int i = 1; i < nw; ++i) v = fmaxf(v, sm[i]);
+    __syncthreads();
+    return v;
+}
+
+__device__ __forceinline__ int block_max_int(int v, int* sm) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, off));
+    __syncthreads();
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int i = 1; i < nw; ++i) v = max(v, sm[i]);
+    __syncthreads();
+    return v;
+}
+
+// Sum over the tile partials of one replica by one warp (fixed order).
+__device__ __forceinline__ double warp_sum_tiles(const Dev& d, const RepDev& R, int slot) {
+    const int lane = threadIdx.x & 31;
+    double s = 0.0;
+    for (int t = lane; t < R.ntiles; t += 32) s += __ldcg(d.part + (size_t)(R.tile_begin + t) * 8 + slot);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    return __shfl_sync(0xffffffffu, s, 0);
+}
+
+__device__ __forceinline__ void decode_cell(int l, const int nc[3], int& cx, int& cy, int& cz) {
+    cz = l % nc[2];
+    const int q = l / nc[2];
+    cy = q % nc[1];
+    cx = q / nc[1];
+}
+
+// FP32 mirror: position relative to the centre of the atom's frozen cell,
+// taken to the nearest periodic image (continuous while the atom stays near
+// its cell; in brute mode the "cell" is the whole box, so it is the wrapped
+// position relative to the box centre).
+__device__ __forceinline__ float4 mirror_of(double4 p, int cell_local, const RepDev& R) {
+    int cx, cy, cz;
+    decode_cell(cell_local, R.nc, cx, cy, cz);
+    const double c[3] = {((double)cx + 0.5) * R.cs[0], ((double)cy + 0.5) * R.cs[1],
+                         ((double)cz + 0.5) * R.cs[2]};
+    const double x[3] = {p.x, p.y, p.z};
+    float o[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double u = x[a] - c[a];
+        const double h = 0.5 * R.box[a];
+        if (u >= h) u -= R.box[a];
+        else if (u < -h) u += R.box[a];
+        o[a] = (float)u;
+    }
+    return make_float4(o[0], o[1], o[2], __int_as_float(type_of(p)));
+}
+
+// ---------------------------------------------------------------------------
+// Tree-order reductions over atoms of type `sel`.
+// Pass 1 slots: 0-2 sum(v*m), 3 sum(1*m), 4 sum(temp), 5 sum(m*(v.v)/2),
+//               6 sum(potential), 7 count.
+__device__ void phase_partials1(const Dev& d, int sel) {
+    __shared__ double sm[8 * 32];
+    const int N = d.ntot;
+    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
+        const int4 tl = d.tiles[t];
+        const int s = tl.y + threadIdx.x;
+        double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if ((int)threadIdx.x < tl.z) {
+            const double4 p = ldcg4(d.pos + s);
+            const int ty = type_of(p);
+            if (ty == sel) {
+                const double m = d.mass[ty];
+                const double vx = __ldcg(d.vel + s), vy = __ldcg(d.vel + N + s),
+                             vz = __ldcg(d.vel + 2 * N + s);
+                v[0] = vx * m; v[1] = vy * m; v[2] = vz * m; v[3] = 1.0 * m;
+                v[4] = __ldcg(d.evir + s);
+                v[5] = m * (vx * vx + vy * vy + vz * vz) / 2.0;
+                v[6] = __ldcg(d.epot + s);
+                v[7] = 1.0;
+            }
+        }
+        block_sum<8>(v, sm);
+        if (threadIdx.x == 0)
+            for (int k = 0; k < 8; ++k) d.part[(size_t)t * 8 + k] = v[k];
+    }
+}
+
+// One warp per replica.
+__device__ void phase_finalize1(const Dev& d) {
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int r = gw; r < d.nrep; r += warps) {
+        const RepDev R = load_rep(d.rep + r);
+        double S[8];
+        for (int k = 0; k < 8; ++k) S[k] = warp_sum_tiles(d, R, k);
+        if ((threadIdx.x & 31) == 0) {
+            RepDev* W = d.rep + r;
+            W->vcm[0] = S[0] / S[3]; W->vcm[1] = S[1] / S[3]; W->vcm[2] = S[2] / S[3];
+            W->mom[0] = S[0]; W->mom[1] = S[1]; W->mom[2] = S[2];
+            W->msum = S[3]; W->virsum = S[4]; W->ke = S[5]; W->pe = S[6] / 2.0;
+            W->count = (long long)S[7];
+        }
+    }
+}
+
+// Pass 2 slots: 0 sum(m*|v-vcm|^2/2), 1 sum(m dvx dvx + m dvy dvy + m dvz dvz)
+__device__ void phase_partials2(const Dev& d, int sel) {
+    __shared__ double sm[2 * 32];
+    const int N = d.ntot;
+    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
+        const int4 tl = d.tiles[t];
+        const int s = tl.y + threadIdx.x;
+        double v[2] = {0, 0};
+        if ((int)threadIdx.x < tl.z) {
+            const double4 p = ldcg4(d.pos + s);
+            const int ty = type_of(p);
+            if (ty == sel) {
+                const double vc0 = __ldcg(&d.rep[tl.x].vcm[0]), vc1 = __ldcg(&d.rep[tl.x].vcm[1]),
+                             vc2 = __ldcg(&d.rep[tl.x].vcm[2]);
+                const double m = d.mass[ty];
+                const double dx = __ldcg(d.vel + s) - vc0, dy = __ldcg(d.vel + N + s) - vc1,
+                             dz = __ldcg(d.vel + 2 * N + s) - vc2;
+                v[0] = m * (dx * dx + dy * dy + dz * dz) / 2.0;
+                v[1] = m * dx * dx + m * dy * dy + m * dz * dz;
+            }
+        }
+        block_sum<2>(v, sm);
+        if (threadIdx.x == 0) {
+            d.part[(size_t)t * 8 + 0] = v[0];
+            d.part[(size_t)t * 8 + 1] = v[1];
+        }
+    }
+}
+
+// temperature.rs:4-7
+__device__ __forceinline__ double temperature_of(double thermal, long long n) {
+    const double t = (2.0 * thermal) / (3.0 * (double)n * K_B);
+    return t * 100.0;
+}
+
+// Coupling factors from the reduced T and P (thermostat.rs:31-39, barostat.rs:29-30).
+__device__ __forceinline__ void coupling_factors(RepDev* W, const RepDev& R, double T, double P,
+                                                 double dt) {
+    if (R.thermo_on) {
+        if (R.thermo_kind == 0) {
+            const double l2 = 1.0 + dt / R.th_tau * (R.th_T0 / T - 1.0);
+            W->lambda = sqrt(l2);
+        } else {
+            const double psi_dot = -((R.th_T0 / T) - 1.0) / R.th_tau;
+            const double psi = R.psi + psi_dot * (dt / 2.0);
+            W->psi = psi;
+            W->lambda = exp(-psi * dt / 2.0);
+        }
+    }
+    if (R.baro_on) {
+        const double m3 = 1.0 + dt * R.ba_beta / R.ba_tau * (P - R.ba_P0);
+        W->myu = cbrt(m3);
+    }
+}
+
+// Finalize pass 2.  coupling: first apply the box part of the pending
+// barostat update (box *= mu once per type, barostat.rs:45), then T, P and
+// the coupling factors.
+__device__ void phase_finalize2(const Dev& d, const StepParams& sp, bool coupling) {
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int r = gw; r < d.nrep; r += warps) {
+        const RepDev R = load_rep(d.rep + r);
+        const double th = warp_sum_tiles(d, R, 0);
+        const double p1 = warp_sum_tiles(d, R, 1);
+        if ((threadIdx.x & 31) == 0) {
+            RepDev* W = d.rep + r;
+            double box[3] = {R.box[0], R.box[1], R.box[2]};
+            if (coupling && R.pending != 1.0) {
+                for (int k = 0; k < d.ntypes; ++k)
+                    for (int a = 0; a < 3; ++a) box[a] *= R.pending;
+                for (int a = 0; a < 3; ++a) { W->box[a] = box[a]; W->cs[a] = box[a] / (double)R.nc[a]; }
+            }
+            const double volume = box[0] * box[1] * box[2];
+            const double T = temperature_of(th, R.count);
+            const double P = (p1 + (-R.virsum) * 0.5) / volume / 3.0;
+            W->thermal = th; W->T = T; W->P = P;
+            if (coupling) coupling_factors(W, R, T, P, sp.dt);
+        }
+    }
+}
+
+// Reference-order reductions: one thread per replica walks the atoms of type
+// `sel` in the reference's order and sums serially, exactly as the iterator
+// folds of macro_parameters/*.rs do.
+__device__ void phase_serial(const Dev& d, const StepParams& sp, int sel, bool coupling) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = gridDim.x * blockDim.x;
+    const int N = d.ntot;
+    for (int r = gt; r < d.nrep; r += nt) {
+        const RepDev R = load_rep(d.rep + r);
+        RepDev* W = d.rep + r;
+        const long long b = R.begin + R.type_off[sel], e = R.begin + R.type_off[sel + 1];
+        const double m = d.mass[sel];
+        double sx = 0, sy = 0, sz = 0, sw = 0, ke = 0, pe = 0;
+        for (long long k = b; k < e; ++k) {
+            const int s = __ldcg(d.slot_of_rank + k);
+            if (s < 0 || s >= N) { atomicOr(d.err, E_BOUNDS); continue; }
+            const double vx = __ldcg(d.vel + s), vy = __ldcg(d.vel + N + s), vz = __ldcg(d.vel + 2 * N + s);
+            sx += vx * m; sy += vy * m; sz += vz * m; sw += 1.0 * m;   // mod.rs:12-25
+            ke += m * (vx * vx + vy * vy + vz * vz) / 2.0;              // energy.rs:14-22
+            pe += __ldcg(d.epot + s);                                    // energy.rs:40-49
+        }
+        const double vc[3] = {sx / sw, sy / sw, sz / sw};
+        double th = 0, r1 = 0, r2 = 0;
+        for (long long k = b; k < e; ++k) {
+            const int s = __ldcg(d.slot_of_rank + k);
+            if (s < 0 || s >= N) continue;
+            const double dx = __ldcg(d.vel + s) - vc[0], dy = __ldcg(d.vel + N + s) - vc[1],
+                         dz = __ldcg(d.vel + 2 * N + s) - vc[2];
+            th += m * (dx * dx + dy * dy + dz * dz) / 2.0;             // energy.rs:25-37
+            r1 += m * dx * dx; r1 += m * dy * dy; r1 += m * dz * dz;   // pressure.rs:13-18
+            r2 -= __ldcg(d.evir + s);
+        }
+        double box[3] = {R.box[0], R.box[1], R.box[2]};
+        if (coupling && R.pending != 1.0) {
+            for (int k = 0; k < d.ntypes; ++k)
+                for (int a = 0; a < 3; ++a) box[a] *= R.pending;
+            for (int a = 0; a < 3; ++a) { W->box[a] = box[a]; W->cs[a] = box[a] / (double)R.nc[a]; }
+        }
+        const double volume = box[0] * box[1] * box[2];
+        const double T = temperature_of(th, e - b);
+        const double P = (r1 + r2 * 0.5) / volume / 3.0;
+        W->vcm[0] = vc[0]; W->vcm[1] = vc[1]; W->vcm[2] = vc[2];
+        W->mom[0] = sx; W->mom[1] = sy; W->mom[2] = sz;
+        W->msum = sw; W->ke = ke; W->pe = pe / 2.0; W->thermal = th; W->virsum = -r2;
+        W->count = e - b; W->T = T; W->P = P;
+        if (coupling) coupling_factors(W, R, T, P, sp.dt);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Drift: integrator.rs:30-47 for every atom; mirror + displacement.
+__device__ void phase_drift(const Dev& d, const StepParams& sp) {
+    __shared__ float smx[32];
+    const int N = d.ntot;
+    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
+        const int4 tl = d.tiles[t];
+        const RepDev R = load_rep(d.rep + tl.x);
+        const int s = tl.y + threadIdx.x;
+        float disp = 0.f;
+        if ((int)threadIdx.x < tl.z) {
+            double4 p = d.pos[s];
+            if (sp.do_drift) {
+                const int ty = type_of(p);
+                const double c = sp.kick_c[ty];
+                double vx = d.vel[s], vy = d.vel[N + s], vz = d.vel[2 * N + s];
+                vx = __dadd_rn(vx, __dmul_rn(d.frc[s], c));             // :30-36 kick
+                vy = __dadd_rn(vy, __dmul_rn(d.frc[N + s], c));
+                vz = __dadd_rn(vz, __dmul_rn(d.frc[2 * N + s], c));
+                if (R.thermo_on) {                                       // thermostat.rs:54-58
+                    vx = __dmul_rn(vx, R.lambda); vy = __dmul_rn(vy, R.lambda);
+                    vz = __dmul_rn(vz, R.lambda);
+                }
+                d.vel[s] = vx; d.vel[N + s] = vy; d.vel[2 * N + s] = vz;
+                double x = p.x, y = p.y, z = p.z;
+                if (R.pending != 1.0) {                                  // barostat.rs:46-48
+                    x = __dmul_rn(x, R.pending); y = __dmul_rn(y, R.pending);
+                    z = __dmul_rn(z, R.pending);
+                }
+                x = __dadd_rn(x, __dmul_rn(vx, sp.dt));                   // :42-46 drift
+                y = __dadd_rn(y, __dmul_rn(vy, sp.dt));
+                z = __dadd_rn(z, __dmul_rn(vz, sp.dt));
+                // core/src/particle.rs:120-141: a single shift per axis
+                if (x < 0.0) x = __dadd_rn(x, R.box[0]); else if (x >= R.box[0]) x = __dsub_rn(x, R.box[0]);
+                if (y < 0.0) y = __dadd_rn(y, R.box[1]); else if (y >= R.box[1]) y = __dsub_rn(y, R.box[1]);
+                if (z < 0.0) z = __dadd_rn(z, R.box[2]); else if (z >= R.box[2]) z = __dsub_rn(z, R.box[2]);
+                p.x = x; p.y = y; p.z = z;
+                d.pos[s] = p;
+            }
+            const int cl = d.cell[s] - R.cell_base;
+            // cl is out of range only before the first binning (fresh upload);
+            // the forced rebuild that follows computes the mirror then.
+            if (cl >= 0 && cl < R.nc[0] * R.nc[1] * R.nc[2]) {
+                const float4 m = mirror_of(p, cl, R);
+                d.mir[s] = m;
+                const float4 m0 = d.mir0[s];
+                const float sc = (float)(R.box[0] / R.box_build[0]);
+                const float L[3] = {(float)R.box[0], (float)R.box[1], (float)R.box[2]};
+                float dd[3] = {m.x - sc * m0.x, m.y - sc * m0.y, m.z - sc * m0.z};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    if (dd[a] > 0.5f * L[a]) dd[a] -= L[a];
+                    else if (dd[a] < -0.5f * L[a]) dd[a] += L[a];
+                }
+                disp = sqrtf(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+            }
+        }
+        disp = block_max(disp, smx);
+        if (threadIdx.x == 0) atomicMax(&d.rep[tl.x].max_disp_bits, __float_as_uint(disp));
+    }
+}
+
+// Per replica: consume the pending barostat factor, decide on a rebuild.
+__device__ void phase_decide(const Dev& d, const StepParams& sp) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = gridDim.x * blockDim.x;
+    for (int r = gt; r < d.nrep; r += nt) {
+        const RepDev R = load_rep(d.rep + r);
+        RepDev* W = d.rep + r;
+        int steps_since = R.steps_since;
+        if (sp.do_drift) {
+            W->pending = R.baro_on ? R.myu : 1.0;
+            ++steps_since;
+        }
+        const double sc = R.box[0] / R.box_build[0];
+        const double maxd = (double)__uint_as_float(R.max_disp_bits);
+        // A pair outside the list at the rebuild had r0 >= rlist; it is now at
+        // >= sc*rlist - 2*maxd, which must stay above the largest cutoff.
+        const bool need = sp.force_rebuild || R.rebuild ||
+                          (2.0 * maxd > sc * d.rlist - d.rcmax - 1e-5 * d.rlist) ||
+                          (sp.fixed_interval > 0 && steps_since >= sp.fixed_interval);
+        if (need) {
+            long long nc[3];
+            bool brute = R.cell_cap < 27;
+            for (int a = 0; a < 3; ++a) {
+                nc[a] = (long long)floor(R.box[a] / (d.rlist * (1.0 + 1e-6)));
+                if (nc[a] < 3) brute = true;
+            }
+            if (!brute) {
+                while (nc[0] * nc[1] * nc[2] > (long long)R.cell_cap) {
+                    int a = 0;
+                    if (nc[1] > nc[a]) a = 1;
+                    if (nc[2] > nc[a]) a = 2;
+                    --nc[a];
+                }
+                if (nc[0] < 3 || nc[1] < 3 || nc[2] < 3) brute = true;
+            }
+            if (brute) nc[0] = nc[1] = nc[2] = 1;
+            for (int a = 0; a < 3; ++a) {
+                W->nc[a] = (int)nc[a];
+                W->cs[a] = R.box[a] / (double)nc[a];
+                W->box_build[a] = R.box[a];
+            }
+            W->mode = brute ? MODE_BRUTE : MODE_CELLS;
+            W->max_disp_bits = 0u;
+            W->max_nn = 0;
+            steps_since = 0;
+            W->rebuild = 1;
+            atomicAdd(d.bar + 2, 1u);
+        } else {
+            W->rebuild = 0;
+        }
+        W->steps_since = steps_since;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Rebuild phases (only tiles/cells of replicas with rebuild set do work).
+
+__device__ void phase_zero_cells(const Dev& d) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = gridDim.x * blockDim.x;
+    for (int c = gt; c < d.ncells; c += nt) {
+        const int r = d.cell_rep[c];
+        if (__ldcg(&d.rep[r].rebuild)) { d.cell_count[c] = 0; d.cell_fill[c] = 0; }
+    }
+}
+
+__device__ void phase_bin(const Dev& d) {
+    const int N = d.ntot;
+    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
+        const int4 tl = d.tiles[t];
+        const RepDev R = load_rep(d.rep + tl.x);
+        if (!R.rebuild) continue;
+        const int s = tl.y + threadIdx.x;
+        if ((int)threadIdx.x >= tl.z) continue;
+        const double4 p = d.pos[s];
+        int local = 0;
+        if (R.mode == MODE_CELLS) {
+            const double x[3] = {p.x, p.y, p.z};
+            int c[3];
+            for (int a = 0; a < 3; ++a) {
+                const double inv = (double)R.nc[a] / R.box[a];
+                int ci = (int)floor(x[a] * inv);
+                c[a] = min(max(ci, 0), R.nc[a] - 1);
+            }
+            local = (c[0] * R.nc[1] + c[1]) * R.nc[2] + c[2];
+        }
+        const int cell = R.cell_base + local;
+        d.tmp_i[2 * (size_t)N + s] = cell;
+        atomicAdd(d.cell_count + cell, 1);
+    }
+}
+
+// Exclusive scan of cell counts over all cells (block chunks + block sums).
+__device__ void phase_scan_a(const Dev& d, int chunk) {
+    __shared__ double sm[32];
+    const int b0 = blockIdx.x * chunk, b1 = min(b0 + chunk, d.ncells);
+    double v[1] = {0.0};
+    for (int c = b0 + threadIdx.x; c < b1; c += blockDim.x) v[0] += (double)__ldcg(d.cell_count + c);
+    block_sum<1>(v, sm);
+    if (threadIdx.x == 0) d.bsum[blockIdx.x] = (int)v[0];
+}
+
+__device__ void phase_scan_b(const Dev& d) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int run = 0;
+        for (int b = 0; b < (int)gridDim.x; ++b) {
+            const int v = __ldcg(d.bsum + b);
+            d.bsum[b] = run;
+            run += v;
+        }
+        d.cell_start[d.ncells] = run;
+    }
+}
+
+__device__ void phase_scan_c(const Dev& d, int chunk) {
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    const int b0 = blockIdx.x * chunk, b1 = min(b0 + chunk, d.ncells);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) carry = __ldcg(d.bsum + blockIdx.x);
+    __syncthreads();
+    for (int base = b0; base < b1; base += blockDim.x) {
+        const int c = base + threadIdx.x;
+        const int x = (c < b1) ? __ldcg(d.cell_count + c) : 0;
+        int inc = x;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += y;
+        }
+        if (lane == 31) wsum[w] = inc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int run = 0;
+            for (int i = 0; i < nw; ++i) { const int t = wsum[i]; wsum[i] = run; run += t; }
+        }
+        __syncthreads();
+        if (c < b1) d.cell_start[c] = carry + wsum[w] + inc - x;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += wsum[w] + inc;
+        __syncthreads();
+    }
+}
+
+__device__ void phase_scatter(const Dev& d) {
+    const int N = d.ntot;
+    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
+        const int4 tl = d.tiles[t];
+        const RepDev R = load_rep(d.rep + tl.x);
+        if (!R.rebuild) continue;
+        const int s = tl.y + threadIdx.x;
+        if ((int)threadIdx.x >= tl.z) continue;
+        const int cell = d.tmp_i[2 * (size_t)N + s];
+        if (cell < R.cell_base || cell >= R.cell_base + R.cell_cap) { atomicOr(d.err, E_CELLS); continue; }
+        const int slot = __ldcg(d.cell_start + cell) + atomicAdd(d.cell_fill + cell, 1);
+        if (slot < R.begin || slot >= R.begin + R.n) { atomicOr(d.err, E_CELLS); continue; }
+        d.perm[slot] = s;
+        d.tmp_pos[s] = d.pos[s];
+        for (int k = 0; k < 3; ++k) {
+            d.tmp_d[(size_t)k * N + s] = d.vel[(size_t)k * N + s];
+            d.tmp_d[(size_t)(3 + k) * N + s] = d.frc[(size_t)k * N + s];
+        }
+        d.tmp_d[(size_t)6 * N + s] = d.epot[s];
+        d.tmp_d[(size_t)7 * N + s] = d.evir[s];
+        d.tmp_i[s] = d.orig[s];
+        d.tmp_i[(size_t)N + s] = d.rank[s];
+    }
+}
+
+// Canonical order inside each cell: ascending caller index (insertion sort).
+__device__ void phase_sort_cells(const Dev& d) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = gridDim.x * blockDim.x;
+    const int N = d.ntot;
+    for (int c = gt; c < d.ncells; c += nt) {
+        const int r = d.cell_rep[c];
+        if (!__ldcg(&d.rep[r].rebuild)) continue;
+        const int b = __ldcg(d.cell_start + c), n = __ldcg(d.cell_count + c);
+        if (b < 0 || n < 0 || b + n > N) { atomicOr(d.err, E_CELLS); continue; }
+        for (int a = 1; a < n; ++a) {
+            const int e = __ldcg(d.perm + b + a);
+            if (e < 0 || e >= N) { atomicOr(d.err, E_BOUNDS); break; }
+            const int key = __ldcg(d.tmp_i + e);
+            int k = a - 1;
+            while (k >= 0) {
+                const int f = __ldcg(d.perm + b + k);
+                if (f < 0 || f >= N || __ldcg(d.tmp_i + f) <= key) break;
+                d.perm[b + k + 1] = f;
+                --k;
+            }
+            d.perm[b + k + 1] = e;
+        }
+    }
+}
+
+__device__ void phase_gather(const Dev& d) {
+    const int N = d.ntot;
+    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
+        const int4 tl = d.tiles[t];
+        const RepDev R = load_rep(d.rep + tl.x);
+        if (!R.rebuild) continue;
+        const int s = tl.y + threadIdx.x;
+        if ((int)threadIdx.x >= tl.z) continue;
+        const int i = __ldcg(d.perm + s);
+        if (i < R.begin || i >= R.begin + R.n) { atomicOr(d.err, E_BOUNDS); continue; }
+        const double4 p = ldcg4(d.tmp_pos + i);
+        d.pos[s] = p;
+        for (int k = 0; k < 3; ++k) {
+            d.vel[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)k * N + i);
+            d.frc[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)(3 + k) * N + i);
+        }
+        d.epot[s] = __ldcg(d.tmp_d + (size_t)6 * N + i);
+        d.evir[s] = __ldcg(d.tmp_d + (size_t)7 * N + i);
+        d.orig[s] = __ldcg(d.tmp_i + i);
+        const int rk = __ldcg(d.tmp_i + (size_t)N + i);
+        d.rank[s] = rk;
+        const int cell = __ldcg(d.tmp_i + 2 * (size_t)N + i);
+        d.cell[s] = cell;
+        const float4 m = mirror_of(p, cell - R.cell_base, R);
+        d.mir[s] = m;
+        d.mir0[s] = m;
+        if (rk >= 0 && rk < N) d.slot_of_rank[rk] = s;
+        else atomicOr(d.err, E_BOUNDS);
+    }
+}
+
+// Verlet neighbour list with skin: every j (of type >= type i, the
+// reference's t1 <= t2 loop, potential.rs:171-172) within rlist of i.
+__device__ void phase_build_list(const Dev& d) {
+    __shared__ int smi[32];
+    const int N = d.ntot, cap = d.cap, tpa = d.tpa;
+    const float rl = (float)(d.rlist * (1.0 + 1e-5));
+    const float rl2 = rl * rl;
+    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
+        const int4 tl = d.tiles[t];
+        const RepDev R = load_rep(d.rep + tl.x);
+        if (!R.rebuild) continue;
+        const int s = tl.y + threadIdx.x;
+        int cnt = 0;
+        if ((int)threadIdx.x < tl.z) {
+            const float4 xi = __ldcg(d.mir + s);
+            const int ti = type_of(xi);
+            if (R.mode == MODE_CELLS) {
+                int cx, cy, cz;
+                decode_cell(d.cell[s] - R.cell_base, R.nc, cx, cy, cz);
+                const float cs[3] = {(float)R.cs[0], (float)R.cs[1], (float)R.cs[2]};
+                for (int dz = -1; dz <= 1; ++dz) {
+                    int z = cz + dz; z = z < 0 ? z + R.nc[2] : (z >= R.nc[2] ? z - R.nc[2] : z);
+                    for (int dy = -1; dy <= 1; ++dy) {
+                        int y = cy + dy; y = y < 0 ? y + R.nc[1] : (y >= R.nc[1] ? y - R.nc[1] : y);
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            int x = cx + dx; x = x < 0 ? x + R.nc[0] : (x >= R.nc[0] ? x - R.nc[0] : x);
+                            const int cj = R.cell_base + (x * R.nc[1] + y) * R.nc[2] + z;
+                            const uint32_t code = (uint32_t)((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
+                            const float sx = (float)dx * cs[0], sy = (float)dy * cs[1], sz = (float)dz * cs[2];
+                            int jb = __ldcg(d.cell_start + cj), je = jb + __ldcg(d.cell_count + cj);
+                            if (jb < R.begin || je > R.begin + R.n) { atomicOr(d.err, E_CELLS); continue; }
+                            for (int j = jb; j < je; ++j) {
+                                if (j == s) continue;
+                                const float4 xj = __ldcg(d.mir + j);
+                                if (type_of(xj) < ti) continue;
+                                const float ex = xj.x - xi.x + sx, ey = xj.y - xi.y + sy,
+                                            ez = xj.z - xi.z + sz;
+                                if (ex * ex + ey * ey + ez * ez < rl2) {
+                                    if (cnt < cap) d.nbr[nbr_index(s, cnt, tpa, N)] = (uint32_t)j | (code << IDX_BITS);
+                                    ++cnt;
+                                }
+                            }
+                        }
+                    }
+                }
+            } else {
+                const float L[3] = {(float)R.box[0], (float)R.box[1], (float)R.box[2]};
+                for (int j = (int)R.begin; j < (int)R.begin + R.n; ++j) {
+                    if (j == s) continue;
+                    const float4 xj = __ldcg(d.mir + j);
+                    if (type_of(xj) < ti) continue;
+                    float e[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
+                    for (int a = 0; a < 3; ++a) {
+                        if (e[a] < -0.5f * L[a]) e[a] += L[a];
+                        else if (e[a] > 0.5f * L[a]) e[a] -= L[a];
+                    }
+                    if (e[0] * e[0] + e[1] * e[1] + e[2] * e[2] < rl2) {
+                        if (cnt < cap) d.nbr[nbr_index(s, cnt, tpa, N)] = (uint32_t)j | ((uint32_t)CODE_ZERO << IDX_BITS);
+                        ++cnt;
+                    }
+                }
+            }
+            const int n = min(cnt, cap);
+            if (d.refmode) {
+                // the reference's accumulation order: ascending (type, index in type)
+                for (int a = 1; a < n; ++a) {
+                    const uint32_t e = d.nbr[nbr_index(s, a, tpa, N)];
+                    const int key = __ldcg(d.rank + (e & IDX_MASK));
+                    int k = a - 1;
+                    while (k >= 0) {
+                        const uint32_t f = d.nbr[nbr_index(s, k, tpa, N)];
+                        if (__ldcg(d.rank + (f & IDX_MASK)) <= key) break;
+                        d.nbr[nbr_index(s, k + 1, tpa, N)] = f;
+                        --k;
+                    }
+                    d.nbr[nbr_index(s, k + 1, tpa, N)] = e;
+                }
+            }
+            d.nn[s] = n;
+            if (cnt > cap) {
+                atomicOr(d.err, E_NLIST);
+                atomicMax(d.max_needed, cnt);
+            }
+        }
+        const int bm = block_max_int(cnt, smi);
+        if (threadIdx.x == 0) atomicMax(&d.rep[tl.x].max_nn, bm);
+    }
+}
+
+__device__ void phase_rebuild_done(const Dev& d) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = gridDim.x * blockDim.x;
+    for (int r = gt; r < d.nrep; r += nt) {
+        RepDev* W = d.rep + r;
+        if (__ldcg(&W->rebuild)) { W->rebuild = 0; W->nrebuilds += 1; }
+    }
+    if (gt == 0) atomicExch(d.bar + 2, 0u);
+}
+
+// ---------------------------------------------------------------------------
+// The per-step cooperative kernel.  Block = TILE threads.
+__global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
+    if (sp.do_drift && sp.coupled) {
+        const int sel = d.last_type;
+        if (d.refmode) {
+            phase_serial(d, sp, sel, true);
+            grid_barrier(d);
+        } else {
+            phase_partials1(d, sel);
+            grid_barrier(d);
+            phase_finalize1(d);
+            grid_barrier(d);
+            phase_partials2(d, sel);
+            grid_barrier(d);
+            phase_finalize2(d, sp, true);
+            grid_barrier(d);
+        }
+    }
+    phase_drift(d, sp);
+    grid_barrier(d);
+    phase_decide(d, sp);
+    grid_barrier(d);
+    if (*(volatile unsigned int*)(d.bar + 2) == 0u) return;
+    phase_zero_cells(d);
+    grid_barrier(d);
+    phase_bin(d);
+    grid_barrier(d);
+    const int chunk = (d.ncells + gridDim.x - 1) / gridDim.x;
+    phase_scan_a(d, chunk);
+    grid_barrier(d);
+    phase_scan_b(d);
+    grid_barrier(d);
+    phase_scan_c(d, chunk);
+    grid_barrier(d);
+    phase_scatter(d);
+    grid_barrier(d);
+    phase_sort_cells(d);
+    grid_barrier(d);
+    phase_gather(d);
+    grid_barrier(d);
+    phase_build_list(d);
+    grid_barrier(d);
+    phase_rebuild_done(d);
+}
+
+// Macro parameters of type `sel` (solver/src/macro_parameters): results land
+// in the replica records (vcm, mom, ke, pe, thermal, T, P, count).
+__global__ void __launch_bounds__(TILE) k_macro(Dev d, StepParams sp, int sel) {
+    if (d.refmode) {
+        phase_serial(d, sp, sel, false);
+        return;
+    }
+    phase_partials1(d, sel);
+    grid_barrier(d);
+    phase_finalize1(d);
+    grid_barrier(d);
+    phase_partials2(d, sel);
+    grid_barrier(d);
+    phase_finalize2(d, sp, false);
+}
+
+// End of an mdgb_step call: finish the barostat update of the last step
+// (x *= mu; the box part was applied... here as well, once per type).
+__global__ void __launch_bounds__(TILE) k_apply_pending(Dev d) {
+    const int t = blockIdx.x;
+    if (t >= d.ntiles) return;
+    const int4 tl = d.tiles[t];
+    const double f = d.rep[tl.x].pending;
+    if (f == 1.0) return;
+    const int s = tl.y + threadIdx.x;
+    if ((int)threadIdx.x < tl.z) {
+        double4 p = d.pos[s];
+        p.x = __dmul_rn(p.x, f); p.y = __dmul_rn(p.y, f); p.z = __dmul_rn(p.z, f);
+        d.pos[s] = p;
+    }
+}
+
+__global__ void k_apply_pending_box(Dev d) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= d.nrep) return;
+    RepDev* W = d.rep + r;
+    const double f = W->pending;
+    if (f == 1.0) return;
+    for (int k = 0; k < d.ntypes; ++k)
+        for (int a = 0; a < 3; ++a) W->box[a] *= f;
+    for (int a = 0; a < 3; ++a) W->cs[a] = W->box[a] / (double)W->nc[a];
+    W->pending = 1.0;
+}
+
+// Device -> caller order (for download): out[orig[s]] = value[s].
+__global__ void k_gather_out(Dev d, double* out_pos, double* out_vel, double* out_frc,
+                             double* out_pot, double* out_tmp) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.ntot;
+    if (s >= N) return;
+    const int o = d.orig[s];
+    if (o < 0 || o >= N) { atomicOr(d.err, E_BOUNDS); return; }
+    const double4 p = d.pos[s];
+    out_pos[3 * (size_t)o] = p.x; out_pos[3 * (size_t)o + 1] = p.y; out_pos[3 * (size_t)o + 2] = p.z;
+    for (int k = 0; k < 3; ++k) {
+        out_vel[3 * (size_t)o + k] = d.vel[(size_t)k * N + s];
+        out_frc[3 * (size_t)o + k] = d.frc[(size_t)k * N + s];
+    }
+    out_pot[o] = d.epot[s];
+    out_tmp[o] = d.evir[s];
+}
+
+// Caller order -> device (upload): the device order starts as the caller's;
+// the first rebuild sorts it by cell.
+__global__ void k_scatter_in(Dev d, const double* in_pos, const double* in_vel, const int* in_type,
+                             const int* in_rank) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.ntot;
+    if (s >= N) return;
+    double4 p;
+    p.x = in_pos[3 * (size_t)s]; p.y = in_pos[3 * (size_t)s + 1]; p.z = in_pos[3 * (size_t)s + 2];
+    p.w = __longlong_as_double((long long)in_type[s]);
+    d.pos[s] = p;
+    for (int k = 0; k < 3; ++k) {
+        d.vel[(size_t)k * N + s] = in_vel ? in_vel[3 * (size_t)s + k] : 0.0;
+        d.frc[(size_t)k * N + s] = 0.0;
+    }
+    d.epot[s] = 0.0;
+    d.evir[s] = 0.0;
+    d.orig[s] = s;
+    d.rank[s] = in_rank[s];
+    d.slot_of_rank[in_rank[s]] = s;
+    d.cell[s] = -1;
+    d.nn[s] = 0;
+    d.mir0[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Caller order -> device order for force, potential, temp (mdgb_upload_forces).
+__global__ void k_scatter_forces(Dev d, const double* in_frc, const double* in_pot, const double* in_tmp) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.ntot;
+    if (s >= N) return;
+    const int o = d.orig[s];
+    if (o < 0 || o >= N) { atomicOr(d.err, E_BOUNDS); return; }
+    if (in_frc)
+        for (int k = 0; k < 3; ++k) d.frc[(size_t)k * N + s] = in_frc[3 * (size_t)o + k];
+    if (in_pot) d.epot[s] = in_pot[o];
+    if (in_tmp) d.evir[s] = in_tmp[o];
+}
+
+// Interacting pairs from the neighbour list, decided with the reference's
+// FP64 arithmetic (potential.rs:181-204), in caller indices.
+__global__ void k_pairs(Dev d, long long capacity, int* out_i, int* out_j, unsigned long long* count) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = d.ntot;
+    if (s >= N) return;
+    int r = 0;
+    {
+        // replica of s: tiles are contiguous per replica
+        int lo = 0, hi = d.nrep - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (d.rep[mid].begin <= s) lo = mid; else hi = mid - 1;
+        }
+        r = lo;
+    }
+    const RepDev& R = d.rep[r];
+    const double4 pi = d.pos[s];
+    const int ti = type_of(pi);
+    const int n = d.nn[s];
+    for (int k = 0; k < n; ++k) {
+        const uint32_t e = d.nbr[nbr_index(s, k, d.tpa, N)];
+        const int j = (int)(e & IDX_MASK);
+        if (j < 0 || j >= N) { atomicOr(d.err, E_BOUNDS); continue; }
+        const double4 pj = d.pos[j];
+        const PairDev& P = d.pair[ti * MAX_TYPES + type_of(pj)];
+        double rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
+        if (rx < -(R.box[0] / 2.0)) rx += R.box[0]; else if (rx > R.box[0] / 2.0) rx -= R.box[0];
+        if (ry < -(R.box[1] / 2.0)) ry += R.box[1]; else if (ry > R.box[1] / 2.0) ry -= R.box[1];
+        if (rz < -(R.box[2] / 2.0)) rz += R.box[2]; else if (rz > R.box[2] / 2.0) rz -= R.box[2];
+        const double ra = sqrt(rx * rx + ry * ry + rz * rz);
+        if (ra > P.rc) continue;
+        const unsigned long long slot = atomicAdd(count, 1ull);
+        if ((long long)slot < capacity) {
+            out_i[slot] = d.orig[s];
+            out_j[slot] = d.orig[j];
+        }
+    }
+}
+
+}  // namespace mdgb

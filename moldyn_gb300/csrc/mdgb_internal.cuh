@@ -1,0 +1,145 @@
+// mdgb_internal.cuh -- device data layout of the GB300 MD step engine.
+//
+// One engine holds R >= 1 independent replicas (a single system is R = 1).
+// Atoms of replica r occupy the contiguous device range [begin_r, begin_r+n_r)
+// and are kept sorted by cell (counting sort at every list rebuild), so the
+// atoms a tile reads as neighbours sit close together in HBM/L2.  All
+// per-atom work is organised in tiles of TILE atoms that never straddle a
+// replica; kernels take tiles as their unit of work.
+//
+// HBM layout, per atom (sorted order):
+//   pos   double4  FP64 master position, .w carries the type id bits
+//   vel   double   SoA [3][N]
+//   frc   double   SoA [3][N]       force of the last evaluation
+//   epot  double   [N]              the reference's Particle::potential
+//   evir  double   [N]              the reference's Particle::temp (sum of f.r)
+//   mir   float4   FP32 mirror: position relative to the centre of the atom's
+//                  (frozen) cell, .w = type bits -- the mixed path's gather
+//   mir0  float4   mirror at the last rebuild (displacement check)
+//   cell  int      frozen cell (global index)
+//   orig  int      index of the atom in the caller's flat array
+//   rank  int      reference order: type-major index (particles[t][k])
+//   nn    int      neighbour count;  nbr uint32 [cap][N] (tpa-interleaved)
+// A neighbour entry is (j | code << 27): j the sorted index, code in 0..26
+// the periodic cell shift (dx,dy,dz in -1..1) used by the mixed path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mdgb {
+
+constexpr int MAX_TYPES = 16;
+constexpr int TILE = 128;
+constexpr int IDX_BITS = 27;
+constexpr uint32_t IDX_MASK = (1u << IDX_BITS) - 1u;
+constexpr int CODE_ZERO = 13;  // (0,0,0)
+
+// error bits (device word, read by the host after each chunk)
+enum : int {
+    E_NLIST = 1,      // neighbour list capacity exceeded
+    E_TIMEOUT = 2,    // a bounded grid-barrier wait gave up
+    E_FIXED = 4,      // fixed-point force accumulator out of range
+    E_SKIN = 8,       // fixed rebuild interval let an atom move too far
+    E_BOUNDS = 16,    // an index derived from scratch data was out of range
+    E_CELLS = 32,     // cell bookkeeping inconsistent
+};
+
+enum : int { MODE_CELLS = 0, MODE_BRUTE = 1 };
+
+// Pair potential (Lennard-Jones, potential.rs:12-18).  FP64 fields are the
+// reference's values; FP32 fields feed the mixed path.
+struct PairDev {
+    double sigma, eps, rc, ucut, eps4, eps24;
+    float sig2f, eps4f, eps24f, ucutf;
+    float rc2f_lo, rc2f_hi;  // band around rc^2 decided exactly in FP64
+    int pad0, pad1;
+};
+
+struct RepDev {
+    // static, set at upload
+    long long begin;
+    int n, cell_base, cell_cap, tile_begin, ntiles, last_type_count;
+    int type_off[MAX_TYPES + 1];  // reference order: type t owns ranks [begin+off[t], begin+off[t+1])
+    // geometry (device-updated)
+    double box[3];
+    double box_build[3];
+    double cs[3];
+    int nc[3];
+    int mode;
+    // coupling
+    int thermo_on, thermo_kind, baro_on, pad0;
+    double th_tau, th_T0, lambda, psi;
+    double ba_beta, ba_tau, ba_P0, myu;
+    double pending;        // barostat factor still to apply to positions (1 = none)
+    // rebuild bookkeeping
+    unsigned int max_disp_bits;
+    int rebuild;
+    int steps_since;
+    int nrebuilds;
+    int max_nn;
+    int pad1;
+    // reductions (coupling or macro)
+    double vcm[3], msum, thermal, ke, pe, virsum, T, P, mom[3];
+    long long count;
+};
+
+struct StepParams {
+    double dt;
+    double kick_c[MAX_TYPES];  // dt / (2 m_t), computed on the host as the reference does
+    int coupled;               // any thermostat/barostat active
+    int thermo_nh;             // Nose-Hoover present (two-stage update)
+    int fixed_interval;        // >0: rebuild every that many steps
+    int force_rebuild;         // rebuild every replica now
+    int do_drift;              // 0: only (re)build / refresh, no integration
+};
+
+// Everything a kernel needs, passed by value.
+struct Dev {
+    int ntot, ntiles, nrep, ntypes, cap, tpa, ncells;
+    int refmode, mixed, single_type, last_type;
+    double mass[MAX_TYPES];
+    double rlist, rcmax, skin;
+    float fscale, inv_fscale_f;  // fixed-point scale (power of two)
+    double inv_fscale;
+    double4* pos;
+    double* vel;
+    double* frc;
+    double* epot;
+    double* evir;
+    float4* mir;
+    float4* mir0;
+    int* cell;
+    int* orig;
+    int* rank;
+    int* nn;
+    uint32_t* nbr;
+    int4* tiles;       // (replica, begin, count, 0)
+    RepDev* rep;
+    const PairDev* pair;  // [MAX_TYPES*MAX_TYPES]
+    double* part;      // [ntiles][8] tile partials
+    int* err;
+    int* max_needed;   // largest neighbour count requested
+    // rebuild scratch
+    int* cell_count;
+    int* cell_fill;
+    int* cell_start;   // [ncells+1]
+    int* cell_rep;     // replica of each cell
+    int* perm;
+    double4* tmp_pos;
+    double* tmp_d;     // [8][N]: vel3, frc3, epot, evir
+    int* tmp_i;        // [3][N]: orig, rank, cell
+    int* slot_of_rank;
+    int* bsum;         // [grid] scan block sums
+    unsigned int* bar; // [4] grid barrier: count, generation, any_rebuild, pad
+    unsigned int* queue;  // persistent force kernel work counter
+    int* tile_order;   // persistent kernel tile order (costliest first)
+};
+
+__device__ __forceinline__ int type_of(double4 p) { return (int)__double_as_longlong(p.w); }
+__device__ __forceinline__ int type_of(float4 p) { return __float_as_int(p.w); }
+
+__host__ __device__ __forceinline__ size_t nbr_index(int s, int k, int tpa, int ntot) {
+    return ((size_t)(k / tpa) * (size_t)ntot + (size_t)s) * (size_t)tpa + (size_t)(k % tpa);
+}
+
+}  // namespace mdgb
