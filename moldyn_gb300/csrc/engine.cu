@@ -84,7 +84,7 @@ struct mdgb_engine {
     std::vector<void*> allocs;
     void* nbr_alloc = nullptr;
     // snapshot buffers (chunk retry)
-    double4* snap_pos = nullptr;
+    double4_32a* snap_pos = nullptr;
     double* snap_d = nullptr;   // [8][N]
     int* snap_i = nullptr;      // [4][N]: orig, rank, cell, slot_of_rank
     float4* snap_mir0 = nullptr;
@@ -180,6 +180,7 @@ int upload_pairs(mdgb_engine* e) {
     if (!(fchar > 0.0)) fchar = 1.0;
     const int ex = 31 - (int)std::ceil(std::log2(fchar));
     e->dev.fscale = std::ldexp(1.0f, ex);
+    e->dev.fscale_log2 = ex;
     e->dev.inv_fscale = std::ldexp(1.0, -ex);
     e->dev.inv_fscale_f = std::ldexp(1.0f, -ex);
     e->skin = e->cfg.skin > 0.0 ? e->cfg.skin : 0.12 * e->rcmax;
@@ -313,7 +314,7 @@ int snapshot(mdgb_engine* e, bool restore) {
     };
     Dev& d = e->dev;
     if (!restore) {
-        CU(cp(e->snap_pos, d.pos, N * sizeof(double4)));
+        CU(cp(e->snap_pos, d.pos, N * sizeof(double4_32a)));
         CU(cp(e->snap_d, d.vel, 3 * N * sizeof(double)));
         CU(cp(e->snap_d + 3 * N, d.frc, 3 * N * sizeof(double)));
         CU(cp(e->snap_d + 6 * N, d.epot, N * sizeof(double)));
@@ -325,7 +326,7 @@ int snapshot(mdgb_engine* e, bool restore) {
         CU(cp(e->snap_mir0, d.mir0, N * sizeof(float4)));
         CU(cp(e->snap_rep, d.rep, e->nrep * sizeof(RepDev)));
     } else {
-        CU(cp(d.pos, e->snap_pos, N * sizeof(double4)));
+        CU(cp(d.pos, e->snap_pos, N * sizeof(double4_32a)));
         CU(cp(d.vel, e->snap_d, 3 * N * sizeof(double)));
         CU(cp(d.frc, e->snap_d + 3 * N, 3 * N * sizeof(double)));
         CU(cp(d.epot, e->snap_d + 6 * N, N * sizeof(double)));

@@ -35,7 +35,7 @@ __device__ __forceinline__ void shift_table(float4* tab, const RepDev* R) {
 }
 
 // The reference's FP64 displacement and distance (potential.rs:181-201).
-__device__ __forceinline__ double ref_distance(const double4 pi, const double4 pj, const double* box,
+__device__ __forceinline__ double ref_distance(const double4_32a pi, const double4_32a pj, const double* box,
                                                double& rx, double& ry, double& rz) {
     rx = __dsub_rn(pj.x, pi.x);
     ry = __dsub_rn(pj.y, pi.y);
@@ -46,6 +46,65 @@ __device__ __forceinline__ double ref_distance(const double4 pi, const double4 p
     if (rz < -hz) rz = __dadd_rn(rz, box[2]); else if (rz > hz) rz = __dsub_rn(rz, box[2]);
     const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
     return __dsqrt_rn(r2);
+}
+
+// ---------------------------------------------------------------------------
+// 64-bit fixed-point accumulation without float->int64 conversions (those run
+// on GB300's narrow FP64 pipe).  A term v (float, already scaled to fixed-point
+// units) is split exactly as v = h * 2^23 + l with h = rint(v / 2^23) and
+// l = v - h * 2^23 (|l| <= 2^22, exact in FP32).  Both are rounded to integers
+// by the magic-number method: adding M = 1.5 * 2^23 to a float of magnitude
+// <= 2^22 lands in [2^23, 2^24], where the float's bit pattern is
+// bits(M) + rint(x).  The bit patterns are summed modulo 2^32 and the offset
+// count * bits(M) removed at the end, so
+//     sum_k rint(v_k) = (sum h_k) * 2^23 + sum l_k
+// exactly, in any order, for |v| <= 2^44 (the kernel re-accumulates an atom
+// with exact conversions when one of its terms may be larger).
+constexpr float FIX_MAGIC = 12582912.0f;           // 1.5 * 2^23
+constexpr unsigned FIX_MAGIC_BITS = 0x4B400000u;   // bits of FIX_MAGIC
+constexpr int FIX_FOLD = 256;                      // fold the 32-bit words every 256 terms
+
+struct FixAcc {
+    unsigned hi, lo;
+    int n;
+    long long wide;
+    __device__ __forceinline__ void init() { hi = lo = 0u; n = 0; wide = 0; }
+    __device__ __forceinline__ void fold() {
+        const int h = (int)(hi - (unsigned)n * FIX_MAGIC_BITS);
+        const int l = (int)(lo - (unsigned)n * FIX_MAGIC_BITS);
+        wide += ((long long)h << 23) + (long long)l;
+        hi = lo = 0u;
+        n = 0;
+    }
+    __device__ __forceinline__ void add(float v) {
+        const float t = v * 1.1920928955078125e-07f;   // v * 2^-23, exact
+        const float a = t + FIX_MAGIC;                  // bits: M + rint(t)
+        const float h = a - FIX_MAGIC;                  // rint(t), exact
+        const float l = fmaf(h, -8388608.0f, v);        // v - h * 2^23, exact
+        const float b = l + FIX_MAGIC;                  // bits: M + rint(l)
+        hi += __float_as_uint(a);
+        lo += __float_as_uint(b);
+        if (++n == FIX_FOLD) fold();
+    }
+    __device__ __forceinline__ long long total() {
+        fold();
+        return wide;
+    }
+};
+
+// Exact int64 -> double for |x| < 2^51 (one FP64 add instead of the slower
+// conversion instruction), then scaled by 2^-k through the exponent field.
+__device__ __forceinline__ double fixed_to_double(long long x, int k) {
+    if (x == 0) return 0.0;
+    double d;
+    if (x > -(1LL << 51) && x < (1LL << 51)) {
+        const long long MB = 0x4338000000000000LL;             // bits of 1.5 * 2^52
+        d = __longlong_as_double(x + MB) - 6755399441055744.0;   // exact integer value
+    } else {
+        d = __ll2double_rn(x);
+    }
+    // |d| >= 1, so subtracting k from the exponent keeps it a normal number
+    return __longlong_as_double(__double_as_longlong(d) - ((long long)k << 52));
 }
 
 template <int TPA>
@@ -101,7 +160,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
         double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0, vr = 0.0;
         int ty = 0;
         if (act) {
-            const double4 pi = d.pos[s];
+            const double4_32a pi = d.pos[s];
             const float4 mi = d.mir[s];
             ty = type_of(pi);
             const int n = d.nn[s];
@@ -121,7 +180,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
                     }
                     if (ex * ex + ey * ey + ez * ez > P.rc2f_hi * 1.0001f) continue;
                 }
-                const double4 pj = d.pos[j];
+                const double4_32a pj = d.pos[j];
                 double rx, ry, rz;
                 const double r = ref_distance(pi, pj, box, rx, ry, rz);
                 if (r > P.rc) continue;                                          // :202-204
@@ -161,6 +220,55 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
 }
 
 // ---------------------------------------------------------------------------
+// Mixed path.  The per-pair FP32 maths is shared by the loops below.
+struct PairF {
+    float sig2, eps4, eps24, ucut, rc2_lo, rc2_hi;
+};
+
+__device__ __forceinline__ PairF pairf(const PairDev& P) {
+    return PairF{P.sig2f, P.eps4f, P.eps24f, P.ucutf, P.rc2f_lo, P.rc2f_hi};
+}
+
+// LJ for one pair at displacement (dx,dy,dz): fs = (dU/dr)/r, u = U(r).
+__device__ __forceinline__ void lj_f32(const PairF& P, float r2, float& fs, float& u) {
+    const float r2i = __fdividef(1.0f, r2);
+    const float s2 = P.sig2 * r2i;
+    const float s6 = s2 * s2 * s2;
+    // (24 eps / r^2) s6 (1 - 2 s6) = (dU/dr) / r ;  4 eps s6 (s6 - 1) - u_cut = U
+    fs = P.eps24 * r2i * s6 * fmaf(-2.0f, s6, 1.0f);
+    u = fmaf(P.eps4 * s6, s6 - 1.0f, -P.ucut);
+}
+
+struct MixedAcc {
+    FixAcc ax, ay, az;
+    float pe, vr, gmax;
+    __device__ __forceinline__ void init() {
+        ax.init(); ay.init(); az.init();
+        pe = vr = gmax = 0.f;
+    }
+    __device__ __forceinline__ void add(float dx, float dy, float dz, float r2, float fs, float u, float fscale) {
+        pe += u;
+        vr = fmaf(fs, r2, vr);
+        const float g = fs * fscale;
+        gmax = fmaxf(gmax, fabsf(g));
+        ax.add(dx * g);
+        ay.add(dy * g);
+        az.add(dz * g);
+    }
+};
+
+// The reference's FP64 decision for one pair; on success (dx,dy,dz) is the
+// FP64 displacement rounded to FP32.
+__device__ __forceinline__ bool exact_pair(const Dev& d, const RepDev* R, int s, int j, double rc, float& dx,
+                                           float& dy, float& dz) {
+    const double box[3] = {R->box[0], R->box[1], R->box[2]};
+    double rx, ry, rz;
+    const double r = ref_distance(d.pos[s], d.pos[j], box, rx, ry, rz);
+    if (r > rc) return false;
+    dx = dbl_to_flt_rn(rx); dy = dbl_to_flt_rn(ry); dz = dbl_to_flt_rn(rz);
+    return true;
+}
+
 template <int TPA, bool SINGLE, bool KICK, bool PERSIST>
 __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp) {
     __shared__ float4 tab[27];
@@ -168,8 +276,10 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
     const int N = d.ntot;
     const int a = threadIdx.x / TPA, lane = threadIdx.x % TPA;
     const float fscale = d.fscale;
-    // |dx * fs * fscale| stays below 2^55 for every term, so 256 terms cannot overflow.
-    const float term_limit = 36028797018963968.0f / (float)(d.rlist * 1.01);
+    // each term |dx * g| <= rlist * gmax; the magic-number split is exact up to 2^44
+    const float rl = (float)(d.rlist * 1.01);
+    const float split_limit = 17592186044416.0f / rl;       // 2^44 / rlist
+    const float range_limit = 36028797018963968.0f / rl;    // 2^55 / rlist
     int iter = 0;
     for (;;) {
         const int t = next_tile(d, PERSIST, iter, &s_tile);
@@ -180,17 +290,76 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
         shift_table(tab, R);
         __syncthreads();
         const bool brute = R->mode == MODE_BRUTE;
-        const float Lf[3] = {(float)R->box[0], (float)R->box[1], (float)R->box[2]};
         const int s = tl.y + a;
         const bool act = a < tl.z;
-        long long ax = 0, ay = 0, az = 0;
-        float pe = 0.f, vr = 0.f, fsmax = 0.f;
+        MixedAcc acc;
+        acc.init();
         int ty = 0;
         if (act) {
             const float4 xi = d.mir[s];
             ty = type_of(xi);
-            PairDev P0;
-            if (SINGLE) P0 = d.pair[ty * MAX_TYPES + ty];
+            PairF P0{};
+            if (SINGLE) P0 = pairf(d.pair[ty * MAX_TYPES + ty]);
+            const int n = d.nn[s];
+            if (!brute) {
+                // hot loop: FP32 and integer work only
+                bool band = false;
+                for (int k = lane; k < n; k += TPA) {
+                    const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                    const int j = (int)(e & IDX_MASK);
+                    const float4 xj = __ldg(d.mir + j);
+                    const float4 sh = tab[e >> IDX_BITS];
+                    const float dx = xj.x - xi.x + sh.x, dy = xj.y - xi.y + sh.y, dz = xj.z - xi.z + sh.z;
+                    const PairF P = SINGLE ? P0 : pairf(d.pair[ty * MAX_TYPES + type_of(xj)]);
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 > P.rc2_hi) continue;
+                    if (r2 >= P.rc2_lo) { band = true; continue; }   // decided in FP64 below
+                    float fs, u;
+                    lj_f32(P, r2, fs, u);
+                    acc.add(dx, dy, dz, r2, fs, u, fscale);
+                }
+                if (band) {
+                    // pairs within 1e-5 of r_cut^2: the reference's FP64 decision
+                    for (int k = lane; k < n; k += TPA) {
+                        const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                        const int j = (int)(e & IDX_MASK);
+                        const float4 xj = __ldg(d.mir + j);
+                        const float4 sh = tab[e >> IDX_BITS];
+                        float dx = xj.x - xi.x + sh.x, dy = xj.y - xi.y + sh.y, dz = xj.z - xi.z + sh.z;
+                        const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(xj)];
+                        const PairF P = pairf(PD);
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        if (r2 > P.rc2_hi || r2 < P.rc2_lo) continue;
+                        if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
+                        const float rr2 = dx * dx + dy * dy + dz * dz;
+                        float fs, u;
+                        lj_f32(P, rr2, fs, u);
+                        acc.add(dx, dy, dz, rr2, fs, u, fscale);
+                    }
+                }
+            } else {
+                // brute mode (a box smaller than three list radii): the reference's
+                // FP64 displacement for every pair -- these replicas are tiny
+                for (int k = lane; k < n; k += TPA) {
+                    const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                    const int j = (int)(e & IDX_MASK);
+                    const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(__ldg(d.mir + j))];
+                    float dx, dy, dz;
+                    if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    float fs, u;
+                    lj_f32(pairf(PD), r2, fs, u);
+                    acc.add(dx, dy, dz, r2, fs, u, fscale);
+                }
+            }
+        }
+        long long sx = acc.ax.total(), sy = acc.ay.total(), sz = acc.az.total();
+        if (act && acc.gmax > split_limit) {
+            // a term may exceed the exact range of the split: redo this lane's
+            // terms with exact float -> int64 conversions (very close pairs only)
+            if (acc.gmax > range_limit) atomicOr(d.err, E_FIXED);
+            sx = sy = sz = 0;
+            const float4 xi = d.mir[s];
             const int n = d.nn[s];
             for (int k = lane; k < n; k += TPA) {
                 const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
@@ -198,52 +367,34 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
                 const float4 xj = __ldg(d.mir + j);
                 const float4 sh = tab[e >> IDX_BITS];
                 float dx = xj.x - xi.x + sh.x, dy = xj.y - xi.y + sh.y, dz = xj.z - xi.z + sh.z;
-                bool near_half = false;
+                const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(xj)];
+                const PairF P = pairf(PD);
                 if (brute) {
-                    if (dx < -0.5f * Lf[0]) dx += Lf[0]; else if (dx > 0.5f * Lf[0]) dx -= Lf[0];
-                    if (dy < -0.5f * Lf[1]) dy += Lf[1]; else if (dy > 0.5f * Lf[1]) dy -= Lf[1];
-                    if (dz < -0.5f * Lf[2]) dz += Lf[2]; else if (dz > 0.5f * Lf[2]) dz -= Lf[2];
-                    near_half = fabsf(fabsf(dx) - 0.5f * Lf[0]) < 1e-5f * Lf[0] ||
-                                fabsf(fabsf(dy) - 0.5f * Lf[1]) < 1e-5f * Lf[1] ||
-                                fabsf(fabsf(dz) - 0.5f * Lf[2]) < 1e-5f * Lf[2];
+                    if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
+                } else {
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 > P.rc2_hi) continue;
+                    if (r2 >= P.rc2_lo && !exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
                 }
-                const PairDev& P = SINGLE ? P0 : d.pair[ty * MAX_TYPES + type_of(xj)];
                 const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 > P.rc2f_hi && !near_half) continue;
-                if (r2 >= P.rc2f_lo || near_half) {
-                    // decide with the reference's FP64 arithmetic (potential.rs:181-204)
-                    const double box[3] = {R->box[0], R->box[1], R->box[2]};
-                    double rx, ry, rz;
-                    const double r = ref_distance(d.pos[s], d.pos[j], box, rx, ry, rz);
-                    if (r > P.rc) continue;
-                    dx = (float)rx; dy = (float)ry; dz = (float)rz;
-                }
-                const float rr2 = dx * dx + dy * dy + dz * dz;
-                const float r2i = __fdividef(1.0f, rr2);
-                const float s2 = P.sig2f * r2i;
-                const float s6 = s2 * s2 * s2;
-                // (24 eps / r^2) s6 (1 - 2 s6) = (dU/dr) / r
-                const float fs = P.eps24f * r2i * s6 * fmaf(-2.0f, s6, 1.0f);
-                pe += fmaf(P.eps4f * s6, s6 - 1.0f, -P.ucutf);
-                vr = fmaf(fs, rr2, vr);
+                float fs, u;
+                lj_f32(P, r2, fs, u);
                 const float g = fs * fscale;
-                fsmax = fmaxf(fsmax, fabsf(g));
-                ax += __float2ll_rn(dx * g);
-                ay += __float2ll_rn(dy * g);
-                az += __float2ll_rn(dz * g);
+                sx += __float2ll_rn(dx * g);
+                sy += __float2ll_rn(dy * g);
+                sz += __float2ll_rn(dz * g);
             }
         }
+        float pe = acc.pe, vr = acc.vr;
         if (TPA > 1) {
-            ax = tpa_sum_ll<TPA>(ax); ay = tpa_sum_ll<TPA>(ay); az = tpa_sum_ll<TPA>(az);
+            sx = tpa_sum_ll<TPA>(sx); sy = tpa_sum_ll<TPA>(sy); sz = tpa_sum_ll<TPA>(sz);
             pe = tpa_sum_f<TPA>(pe); vr = tpa_sum_f<TPA>(vr);
-            fsmax = fmaxf(fsmax, 0.f);
         }
-        if (fsmax > term_limit) atomicOr(d.err, E_FIXED);
         if (act && lane == 0) {
-            const double fx = (double)ax * d.inv_fscale, fy = (double)ay * d.inv_fscale,
-                         fz = (double)az * d.inv_fscale;
+            const double fx = fixed_to_double(sx, d.fscale_log2), fy = fixed_to_double(sy, d.fscale_log2),
+                         fz = fixed_to_double(sz, d.fscale_log2);
             d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
-            d.epot[s] = (double)pe; d.evir[s] = (double)vr;
+            d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr);
             if (KICK) {
                 const double c = sp.kick_c[ty];
                 d.vel[s] = __dadd_rn(d.vel[s], __dmul_rn(fx, c));

@@ -40,10 +40,23 @@ __device__ __forceinline__ RepDev load_rep(const RepDev* p) {
     return r;
 }
 
-__device__ __forceinline__ double4 ldcg4(const double4* p) {
+// One replica record per block, in shared memory (phases work tile by tile
+// and a tile never straddles replicas).
+__shared__ RepDev g_tile_rep;
+
+__device__ __forceinline__ const RepDev& tile_rep(const Dev& d, int r) {
+    __syncthreads();  // every thread is done with the previous tile's record
+    const long long* src = reinterpret_cast<const long long*>(d.rep + r);
+    long long* dst = reinterpret_cast<long long*>(&g_tile_rep);
+    for (int i = threadIdx.x; i < (int)(sizeof(RepDev) / 8); i += blockDim.x) dst[i] = __ldcg(src + i);
+    __syncthreads();
+    return g_tile_rep;
+}
+
+__device__ __forceinline__ double4_32a ldcg4(const double4_32a* p) {
     const double2 a = __ldcg(reinterpret_cast<const double2*>(p));
     const double2 b = __ldcg(reinterpret_cast<const double2*>(p) + 1);
-    return make_double4(a.x, a.y, b.x, b.y);
+    return make_double4_32a(a.x, a.y, b.x, b.y);
 }
 
 __device__ __forceinline__ void grid_barrier(const Dev& d) {
@@ -146,22 +159,37 @@ __device__ __forceinline__ void decode_cell(int l, const int nc[3], int& cx, int
 // taken to the nearest periodic image (continuous while the atom stays near
 // its cell; in brute mode the "cell" is the whole box, so it is the wrapped
 // position relative to the box centre).
-__device__ __forceinline__ float4 mirror_of(double4 p, int cell_local, const RepDev& R) {
+__device__ __forceinline__ float4 mirror_of(double4_32a p, int cell_local, const RepDev& R, const float* hL) {
     int cx, cy, cz;
     decode_cell(cell_local, R.nc, cx, cy, cz);
-    const double c[3] = {((double)cx + 0.5) * R.cs[0], ((double)cy + 0.5) * R.cs[1],
-                         ((double)cz + 0.5) * R.cs[2]};
+    // cell centre (c + 0.5) * cs; c + 0.5 is exact in FP32 and converts exactly
+    const double c[3] = {flt_to_dbl((float)cx + 0.5f) * R.cs[0], flt_to_dbl((float)cy + 0.5f) * R.cs[1],
+                         flt_to_dbl((float)cz + 0.5f) * R.cs[2]};
     const double x[3] = {p.x, p.y, p.z};
     float o[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         double u = x[a] - c[a];
-        const double h = 0.5 * R.box[a];
-        if (u >= h) u -= R.box[a];
-        else if (u < -h) u += R.box[a];
-        o[a] = (float)u;
+        float f = dbl_to_flt_rn(u);
+        const float h = hL[a];
+        // nearest image of the atom relative to its cell centre; only atoms that
+        // just crossed the periodic boundary (|u| ~ L) take this branch, far
+        // from the +-L/2 decision edge, so the FP32 comparison decides it
+        if (f >= h) { u -= R.box[a]; f = dbl_to_flt_rn(u); }
+        else if (f < -h) { u += R.box[a]; f = dbl_to_flt_rn(u); }
+        o[a] = f;
     }
     return make_float4(o[0], o[1], o[2], __int_as_float(type_of(p)));
+}
+
+// core/src/particle.rs:120-141 with the comparisons done on the bit patterns:
+// for x >= 0 and L > 0 the signed 64-bit order of the bits is the numeric
+// order, and x < 0.0 is "sign bit set and not -0.0".
+__device__ __forceinline__ double wrap_ref(double x, double L) {
+    const long long b = __double_as_longlong(x);
+    if (b < 0 && b != (long long)0x8000000000000000ull) return __dadd_rn(x, L);
+    if (b >= __double_as_longlong(L)) return __dsub_rn(x, L);
+    return x;
 }
 
 // ---------------------------------------------------------------------------
@@ -176,7 +204,7 @@ __device__ void phase_partials1(const Dev& d, int sel) {
         const int s = tl.y + threadIdx.x;
         double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if ((int)threadIdx.x < tl.z) {
-            const double4 p = ldcg4(d.pos + s);
+            const double4_32a p = ldcg4(d.pos + s);
             const int ty = type_of(p);
             if (ty == sel) {
                 const double m = d.mass[ty];
@@ -222,7 +250,7 @@ __device__ void phase_partials2(const Dev& d, int sel) {
         const int s = tl.y + threadIdx.x;
         double v[2] = {0, 0};
         if ((int)threadIdx.x < tl.z) {
-            const double4 p = ldcg4(d.pos + s);
+            const double4_32a p = ldcg4(d.pos + s);
             const int ty = type_of(p);
             if (ty == sel) {
                 const double vc0 = __ldcg(&d.rep[tl.x].vcm[0]), vc1 = __ldcg(&d.rep[tl.x].vcm[1]),
@@ -348,14 +376,23 @@ __device__ void phase_serial(const Dev& d, const StepParams& sp, int sel, bool c
 // Drift: integrator.rs:30-47 for every atom; mirror + displacement.
 __device__ void phase_drift(const Dev& d, const StepParams& sp) {
     __shared__ float smx[32];
+    __shared__ float tc[7];   // box (FP32), half box, scale since the last rebuild
     const int N = d.ntot;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
-        const RepDev R = load_rep(d.rep + tl.x);
+        const RepDev& R = tile_rep(d, tl.x);
+        if (threadIdx.x == 0) {
+            for (int a = 0; a < 3; ++a) {
+                tc[a] = dbl_to_flt_rn(R.box[a]);
+                tc[3 + a] = 0.5f * tc[a];
+            }
+            tc[6] = dbl_to_flt_rn(R.box[0] / R.box_build[0]);
+        }
+        __syncthreads();
         const int s = tl.y + threadIdx.x;
         float disp = 0.f;
         if ((int)threadIdx.x < tl.z) {
-            double4 p = d.pos[s];
+            double4_32a p = d.pos[s];
             if (sp.do_drift) {
                 const int ty = type_of(p);
                 const double c = sp.kick_c[ty];
@@ -377,9 +414,9 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp) {
                 y = __dadd_rn(y, __dmul_rn(vy, sp.dt));
                 z = __dadd_rn(z, __dmul_rn(vz, sp.dt));
                 // core/src/particle.rs:120-141: a single shift per axis
-                if (x < 0.0) x = __dadd_rn(x, R.box[0]); else if (x >= R.box[0]) x = __dsub_rn(x, R.box[0]);
-                if (y < 0.0) y = __dadd_rn(y, R.box[1]); else if (y >= R.box[1]) y = __dsub_rn(y, R.box[1]);
-                if (z < 0.0) z = __dadd_rn(z, R.box[2]); else if (z >= R.box[2]) z = __dsub_rn(z, R.box[2]);
+                x = wrap_ref(x, R.box[0]);
+                y = wrap_ref(y, R.box[1]);
+                z = wrap_ref(z, R.box[2]);
                 p.x = x; p.y = y; p.z = z;
                 d.pos[s] = p;
             }
@@ -387,16 +424,15 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp) {
             // cl is out of range only before the first binning (fresh upload);
             // the forced rebuild that follows computes the mirror then.
             if (cl >= 0 && cl < R.nc[0] * R.nc[1] * R.nc[2]) {
-                const float4 m = mirror_of(p, cl, R);
+                const float4 m = mirror_of(p, cl, R, tc + 3);
                 d.mir[s] = m;
                 const float4 m0 = d.mir0[s];
-                const float sc = (float)(R.box[0] / R.box_build[0]);
-                const float L[3] = {(float)R.box[0], (float)R.box[1], (float)R.box[2]};
+                const float sc = tc[6];
                 float dd[3] = {m.x - sc * m0.x, m.y - sc * m0.y, m.z - sc * m0.z};
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    if (dd[a] > 0.5f * L[a]) dd[a] -= L[a];
-                    else if (dd[a] < -0.5f * L[a]) dd[a] += L[a];
+                    if (dd[a] > tc[3 + a]) dd[a] -= tc[a];
+                    else if (dd[a] < -tc[3 + a]) dd[a] += tc[a];
                 }
                 disp = sqrtf(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
             }
@@ -476,11 +512,11 @@ __device__ void phase_bin(const Dev& d) {
     const int N = d.ntot;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
-        const RepDev R = load_rep(d.rep + tl.x);
+        const RepDev& R = tile_rep(d, tl.x);
         if (!R.rebuild) continue;
         const int s = tl.y + threadIdx.x;
         if ((int)threadIdx.x >= tl.z) continue;
-        const double4 p = d.pos[s];
+        const double4_32a p = d.pos[s];
         int local = 0;
         if (R.mode == MODE_CELLS) {
             const double x[3] = {p.x, p.y, p.z};
@@ -508,15 +544,28 @@ __device__ void phase_scan_a(const Dev& d, int chunk) {
     if (threadIdx.x == 0) d.bsum[blockIdx.x] = (int)v[0];
 }
 
+// Exclusive scan of the per-block sums by block 0 (each thread a contiguous run).
 __device__ void phase_scan_b(const Dev& d) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    __shared__ int part[TILE];
+    if (blockIdx.x != 0) return;
+    const int G = gridDim.x;
+    const int per = (G + blockDim.x - 1) / blockDim.x;
+    const int b0 = threadIdx.x * per, b1 = min(b0 + per, G);
+    int sum = 0;
+    for (int b = b0; b < b1; ++b) sum += __ldcg(d.bsum + b);
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
         int run = 0;
-        for (int b = 0; b < (int)gridDim.x; ++b) {
-            const int v = __ldcg(d.bsum + b);
-            d.bsum[b] = run;
-            run += v;
-        }
+        for (int i = 0; i < (int)blockDim.x; ++i) { const int t = part[i]; part[i] = run; run += t; }
         d.cell_start[d.ncells] = run;
+    }
+    __syncthreads();
+    int run = part[threadIdx.x];
+    for (int b = b0; b < b1; ++b) {
+        const int v = __ldcg(d.bsum + b);
+        d.bsum[b] = run;
+        run += v;
     }
 }
 
@@ -554,13 +603,15 @@ __device__ void phase_scatter(const Dev& d) {
     const int N = d.ntot;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
-        const RepDev R = load_rep(d.rep + tl.x);
+        const RepDev& R = tile_rep(d, tl.x);
         if (!R.rebuild) continue;
         const int s = tl.y + threadIdx.x;
         if ((int)threadIdx.x >= tl.z) continue;
         const int cell = d.tmp_i[2 * (size_t)N + s];
         if (cell < R.cell_base || cell >= R.cell_base + R.cell_cap) { atomicOr(d.err, E_CELLS); continue; }
-        const int slot = __ldcg(d.cell_start + cell) + atomicAdd(d.cell_fill + cell, 1);
+        // brute mode: one cell holds the whole replica in its current order
+        const int slot = R.mode == MODE_BRUTE ? s
+                                               : __ldcg(d.cell_start + cell) + atomicAdd(d.cell_fill + cell, 1);
         if (slot < R.begin || slot >= R.begin + R.n) { atomicOr(d.err, E_CELLS); continue; }
         d.perm[slot] = s;
         d.tmp_pos[s] = d.pos[s];
@@ -575,28 +626,65 @@ __device__ void phase_scatter(const Dev& d) {
     }
 }
 
-// Canonical order inside each cell: ascending caller index (insertion sort).
+// Canonical order inside each cell: ascending caller index.  One warp per
+// cell; every element's rank is the number of smaller keys (keys are distinct
+// caller indices), found by shuffling the cell's keys across the warp.  Cells
+// of brute-mode replicas are already in canonical (identity) order.
+constexpr int SORT_MAX_PER_LANE = 4;
+
 __device__ void phase_sort_cells(const Dev& d) {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nt = gridDim.x * blockDim.x;
     const int N = d.ntot;
-    for (int c = gt; c < d.ncells; c += nt) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int c = gw; c < d.ncells; c += nw) {
         const int r = d.cell_rep[c];
-        if (!__ldcg(&d.rep[r].rebuild)) continue;
+        if (!__ldcg(&d.rep[r].rebuild) || __ldcg(&d.rep[r].mode) == MODE_BRUTE) continue;
         const int b = __ldcg(d.cell_start + c), n = __ldcg(d.cell_count + c);
-        if (b < 0 || n < 0 || b + n > N) { atomicOr(d.err, E_CELLS); continue; }
-        for (int a = 1; a < n; ++a) {
-            const int e = __ldcg(d.perm + b + a);
-            if (e < 0 || e >= N) { atomicOr(d.err, E_BOUNDS); break; }
-            const int key = __ldcg(d.tmp_i + e);
-            int k = a - 1;
-            while (k >= 0) {
-                const int f = __ldcg(d.perm + b + k);
-                if (f < 0 || f >= N || __ldcg(d.tmp_i + f) <= key) break;
-                d.perm[b + k + 1] = f;
-                --k;
+        if (n <= 1) continue;
+        if (b < 0 || b + n > N) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
+        if (n <= 32 * SORT_MAX_PER_LANE) {
+            int e[SORT_MAX_PER_LANE], key[SORT_MAX_PER_LANE], rank[SORT_MAX_PER_LANE];
+#pragma unroll
+            for (int g = 0; g < SORT_MAX_PER_LANE; ++g) {
+                const int i = g * 32 + lane;
+                e[g] = i < n ? __ldcg(d.perm + b + i) : -1;
+                const bool ok = e[g] >= 0 && e[g] < N;
+                if (i < n && !ok) atomicOr(d.err, E_BOUNDS);
+                key[g] = ok ? __ldcg(d.tmp_i + e[g]) : 0x7FFFFFFF;
+                rank[g] = 0;
             }
-            d.perm[b + k + 1] = e;
+#pragma unroll
+            for (int g2 = 0; g2 < SORT_MAX_PER_LANE; ++g2) {
+                if (g2 * 32 >= n) break;
+                for (int k = 0; k < 32; ++k) {
+                    const int kk = __shfl_sync(0xffffffffu, key[g2], k);
+#pragma unroll
+                    for (int g = 0; g < SORT_MAX_PER_LANE; ++g) rank[g] += (kk < key[g]) ? 1 : 0;
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int g = 0; g < SORT_MAX_PER_LANE; ++g) {
+                const int i = g * 32 + lane;
+                if (i < n && rank[g] < n) d.perm[b + rank[g]] = e[g];
+            }
+            __syncwarp();
+        } else if (lane == 0) {
+            // very crowded cell: serial insertion sort
+            for (int a = 1; a < n; ++a) {
+                const int e0 = __ldcg(d.perm + b + a);
+                if (e0 < 0 || e0 >= N) { atomicOr(d.err, E_BOUNDS); break; }
+                const int k0 = __ldcg(d.tmp_i + e0);
+                int k = a - 1;
+                while (k >= 0) {
+                    const int f = __ldcg(d.perm + b + k);
+                    if (f < 0 || f >= N || __ldcg(d.tmp_i + f) <= k0) break;
+                    d.perm[b + k + 1] = f;
+                    --k;
+                }
+                d.perm[b + k + 1] = e0;
+            }
         }
     }
 }
@@ -605,13 +693,13 @@ __device__ void phase_gather(const Dev& d) {
     const int N = d.ntot;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
-        const RepDev R = load_rep(d.rep + tl.x);
+        const RepDev& R = tile_rep(d, tl.x);
         if (!R.rebuild) continue;
         const int s = tl.y + threadIdx.x;
         if ((int)threadIdx.x >= tl.z) continue;
         const int i = __ldcg(d.perm + s);
         if (i < R.begin || i >= R.begin + R.n) { atomicOr(d.err, E_BOUNDS); continue; }
-        const double4 p = ldcg4(d.tmp_pos + i);
+        const double4_32a p = ldcg4(d.tmp_pos + i);
         d.pos[s] = p;
         for (int k = 0; k < 3; ++k) {
             d.vel[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)k * N + i);
@@ -624,7 +712,9 @@ __device__ void phase_gather(const Dev& d) {
         d.rank[s] = rk;
         const int cell = __ldcg(d.tmp_i + 2 * (size_t)N + i);
         d.cell[s] = cell;
-        const float4 m = mirror_of(p, cell - R.cell_base, R);
+        const float hL[3] = {0.5f * dbl_to_flt_rn(R.box[0]), 0.5f * dbl_to_flt_rn(R.box[1]),
+                             0.5f * dbl_to_flt_rn(R.box[2])};
+        const float4 m = mirror_of(p, cell - R.cell_base, R, hL);
         d.mir[s] = m;
         d.mir0[s] = m;
         if (rk >= 0 && rk < N) d.slot_of_rank[rk] = s;
@@ -641,7 +731,7 @@ __device__ void phase_build_list(const Dev& d) {
     const float rl2 = rl * rl;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
-        const RepDev R = load_rep(d.rep + tl.x);
+        const RepDev& R = tile_rep(d, tl.x);
         if (!R.rebuild) continue;
         const int s = tl.y + threadIdx.x;
         int cnt = 0;
@@ -803,7 +893,7 @@ __global__ void __launch_bounds__(TILE) k_apply_pending(Dev d) {
     if (f == 1.0) return;
     const int s = tl.y + threadIdx.x;
     if ((int)threadIdx.x < tl.z) {
-        double4 p = d.pos[s];
+        double4_32a p = d.pos[s];
         p.x = __dmul_rn(p.x, f); p.y = __dmul_rn(p.y, f); p.z = __dmul_rn(p.z, f);
         d.pos[s] = p;
     }
@@ -829,7 +919,7 @@ __global__ void k_gather_out(Dev d, double* out_pos, double* out_vel, double* ou
     if (s >= N) return;
     const int o = d.orig[s];
     if (o < 0 || o >= N) { atomicOr(d.err, E_BOUNDS); return; }
-    const double4 p = d.pos[s];
+    const double4_32a p = d.pos[s];
     out_pos[3 * (size_t)o] = p.x; out_pos[3 * (size_t)o + 1] = p.y; out_pos[3 * (size_t)o + 2] = p.z;
     for (int k = 0; k < 3; ++k) {
         out_vel[3 * (size_t)o + k] = d.vel[(size_t)k * N + s];
@@ -846,7 +936,7 @@ __global__ void k_scatter_in(Dev d, const double* in_pos, const double* in_vel, 
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.ntot;
     if (s >= N) return;
-    double4 p;
+    double4_32a p;
     p.x = in_pos[3 * (size_t)s]; p.y = in_pos[3 * (size_t)s + 1]; p.z = in_pos[3 * (size_t)s + 2];
     p.w = __longlong_as_double((long long)in_type[s]);
     d.pos[s] = p;
@@ -894,14 +984,14 @@ __global__ void k_pairs(Dev d, long long capacity, int* out_i, int* out_j, unsig
         r = lo;
     }
     const RepDev& R = d.rep[r];
-    const double4 pi = d.pos[s];
+    const double4_32a pi = d.pos[s];
     const int ti = type_of(pi);
     const int n = d.nn[s];
     for (int k = 0; k < n; ++k) {
         const uint32_t e = d.nbr[nbr_index(s, k, d.tpa, N)];
         const int j = (int)(e & IDX_MASK);
         if (j < 0 || j >= N) { atomicOr(d.err, E_BOUNDS); continue; }
-        const double4 pj = d.pos[j];
+        const double4_32a pj = d.pos[j];
         const PairDev& P = d.pair[ti * MAX_TYPES + type_of(pj)];
         double rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
         if (rx < -(R.box[0] / 2.0)) rx += R.box[0]; else if (rx > R.box[0] / 2.0) rx -= R.box[0];

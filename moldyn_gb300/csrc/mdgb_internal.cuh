@@ -8,7 +8,7 @@
 // replica; kernels take tiles as their unit of work.
 //
 // HBM layout, per atom (sorted order):
-//   pos   double4  FP64 master position, .w carries the type id bits
+//   pos   double4_32a  FP64 master position, .w carries the type id bits
 //   vel   double   SoA [3][N]
 //   frc   double   SoA [3][N]       force of the last evaluation
 //   epot  double   [N]              the reference's Particle::potential
@@ -99,9 +99,10 @@ struct Dev {
     int refmode, mixed, single_type, last_type;
     double mass[MAX_TYPES];
     double rlist, rcmax, skin;
-    float fscale, inv_fscale_f;  // fixed-point scale (power of two)
+    float fscale, inv_fscale_f;  // fixed-point scale 2^fscale_log2
     double inv_fscale;
-    double4* pos;
+    int fscale_log2, pad_fs;
+    double4_32a* pos;
     double* vel;
     double* frc;
     double* epot;
@@ -125,7 +126,7 @@ struct Dev {
     int* cell_start;   // [ncells+1]
     int* cell_rep;     // replica of each cell
     int* perm;
-    double4* tmp_pos;
+    double4_32a* tmp_pos;
     double* tmp_d;     // [8][N]: vel3, frc3, epot, evir
     int* tmp_i;        // [3][N]: orig, rank, cell
     int* slot_of_rank;
@@ -135,8 +136,34 @@ struct Dev {
     int* tile_order;   // persistent kernel tile order (costliest first)
 };
 
-__device__ __forceinline__ int type_of(double4 p) { return (int)__double_as_longlong(p.w); }
+__device__ __forceinline__ int type_of(double4_32a p) { return (int)__double_as_longlong(p.w); }
 __device__ __forceinline__ int type_of(float4 p) { return __float_as_int(p.w); }
+
+// IEEE-754 format conversions with integer operations (GB300's float<->double
+// conversion instructions issue on its narrow FP64 pipe).  Written from the
+// binary formats: exponent rebias 1023 <-> 127, mantissa 52 <-> 23 bits.
+//
+// double -> float, round to nearest even, for |x| in [2^-126, 2^128); smaller
+// magnitudes give +-0 (the engine only converts bounded, well-scaled values).
+__device__ __forceinline__ float dbl_to_flt_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    if (mag < 0x3810000000000000ull) return __uint_as_float(sign);  // below 2^-126
+    unsigned long long r = mag >> 29;
+    const unsigned rem = (unsigned)(mag & 0x1FFFFFFFull);
+    r += (rem > 0x10000000u) | ((rem == 0x10000000u) & (unsigned)(r & 1ull));
+    return __uint_as_float((unsigned)(r - (896ull << 23)) | sign);
+}
+
+// float -> double (exact) for normal floats and zero.
+__device__ __forceinline__ double flt_to_dbl(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned mag = u & 0x7FFFFFFFu;
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if (mag == 0u) return __longlong_as_double((long long)sign);
+    return __longlong_as_double((long long)((((unsigned long long)mag << 29) + (896ull << 52)) | sign));
+}
 
 __host__ __device__ __forceinline__ size_t nbr_index(int s, int k, int tpa, int ntot) {
     return ((size_t)(k / tpa) * (size_t)ntot + (size_t)s) * (size_t)tpa + (size_t)(k % tpa);
