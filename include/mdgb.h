@@ -77,6 +77,7 @@ extern "C" {
 #define MDGB_ERR_DEVICE_TIMEOUT 7      /* a bounded device-side wait gave up */
 #define MDGB_ERR_OUT_OF_MEMORY 8
 #define MDGB_ERR_SKIN_VIOLATION 9      /* fixed rebuild interval too long for the motion */
+#define MDGB_ERR_NOALLOC_TOO_LARGE 10  /* n above MDGB_NOALLOC_MAX_ATOMS (mdgb_forces_noalloc) */
 
 /* ---- precision ------------------------------------------------------- */
 #define MDGB_PRECISION_FP64 0  /* plain path: the reference's FP64 arithmetic */
@@ -210,6 +211,27 @@ MDGB_API int mdgb_interacting_pairs(mdgb_engine* e, int64_t capacity, int32_t* o
 MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out);
 MDGB_API int mdgb_reset_stats(mdgb_engine* e);
 MDGB_API int mdgb_synchronize(mdgb_engine* e);
+
+/* ---- allocation-free force evaluation -------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate GPU
+ * memory themselves (a plugin whose host owns all device memory, a loop where
+ * an allocation's implicit synchronisation is not allowed, a fixed memory
+ * budget): Lennard-Jones forces, potential and temp for n atoms of one type,
+ * with the reference's FP64 arithmetic (update_force), using no memory beyond
+ * the caller's buffers and one static device array of about 0.9 MB that every
+ * GPU loading the library holds until exit.
+ *   d_pos      device, 3*n doubles, positions inside [0, box)
+ *   box        host, 3 doubles
+ *   d_force    device, 3*n doubles (out); d_potential, d_temp device, n (out, nullable)
+ *   stream     cudaStream_t (NULL: the default stream); the call only enqueues work
+ * Limits: n <= MDGB_NOALLOC_MAX_ATOMS (else MDGB_ERR_NOALLOC_TOO_LARGE); at most
+ * MDGB_NOALLOC_MAX_CELLS cells (larger boxes use coarser cells).  The first call
+ * on a device looks up the static array's device address: make it before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU race. */
+#define MDGB_NOALLOC_MAX_ATOMS 65536
+#define MDGB_NOALLOC_MAX_CELLS 32768
+MDGB_API int mdgb_forces_noalloc(int64_t n, const double* d_pos, const double box[3], double sigma, double eps,
+                                 double* d_force, double* d_potential, double* d_temp, void* stream);
 
 /* ---- host-only helpers (no GPU) ------------------------------------- */
 /* out = {sigma, eps, r_cut, u_cut} */

@@ -20,7 +20,8 @@ _LIB = None
 MDGB_OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no state uploaded",
           4: "neighbour list overflow", 5: "fixed-point force overflow", 6: "unsupported",
-          7: "device-side wait timed out", 8: "out of device memory", 9: "skin violation"}
+          7: "device-side wait timed out", 8: "out of device memory", 9: "skin violation",
+          10: "too many atoms for the allocation-free entry point"}
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -104,6 +105,8 @@ SIGNATURES = {
     "mdgb_get_stats": (C.c_int, [_E, C.POINTER(CStats)]),
     "mdgb_reset_stats": (C.c_int, [_E]),
     "mdgb_synchronize": (C.c_int, [_E]),
+    "mdgb_forces_noalloc": (C.c_int, [C.c_int64, C.c_void_p, _dp, C.c_double, C.c_double, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]),
     "mdgb_lj_new": (C.c_int, [C.c_double, C.c_double, _dp]),
     "mdgb_lj_eval": (C.c_int, [_dp, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mdgb_lattice": (C.c_int, [C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_double, _dp, _dp]),

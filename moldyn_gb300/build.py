@@ -32,6 +32,7 @@ UNITS = [
     ("kernels_force.cu", []),
     ("engine.cu", []),
     ("host_util.cpp", []),
+    ("noalloc.cu", []),
 ]
 
 
