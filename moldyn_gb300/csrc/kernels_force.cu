@@ -62,20 +62,11 @@ __device__ __forceinline__ double ref_distance(const double4_32a pi, const doubl
 // with exact conversions when one of its terms may be larger).
 constexpr float FIX_MAGIC = 12582912.0f;           // 1.5 * 2^23
 constexpr unsigned FIX_MAGIC_BITS = 0x4B400000u;   // bits of FIX_MAGIC
-constexpr int FIX_FOLD = 256;                      // fold the 32-bit words every 256 terms
+constexpr int FIX_FOLD = 256;                      // most terms per lane the words can hold
 
 struct FixAcc {
     unsigned hi, lo;
-    int n;
-    long long wide;
-    __device__ __forceinline__ void init() { hi = lo = 0u; n = 0; wide = 0; }
-    __device__ __forceinline__ void fold() {
-        const int h = (int)(hi - (unsigned)n * FIX_MAGIC_BITS);
-        const int l = (int)(lo - (unsigned)n * FIX_MAGIC_BITS);
-        wide += ((long long)h << 23) + (long long)l;
-        hi = lo = 0u;
-        n = 0;
-    }
+    __device__ __forceinline__ void init() { hi = lo = 0u; }
     __device__ __forceinline__ void add(float v) {
         const float t = v * 1.1920928955078125e-07f;   // v * 2^-23, exact
         const float a = t + FIX_MAGIC;                  // bits: M + rint(t)
@@ -84,11 +75,13 @@ struct FixAcc {
         const float b = l + FIX_MAGIC;                  // bits: M + rint(l)
         hi += __float_as_uint(a);
         lo += __float_as_uint(b);
-        if (++n == FIX_FOLD) fold();
     }
-    __device__ __forceinline__ long long total() {
-        fold();
-        return wide;
+    // n terms added: remove the n magic offsets.  With n <= FIX_FOLD the two
+    // 32-bit words cannot overflow (|h| <= 2^21, |l| <= 2^22 per term).
+    __device__ __forceinline__ long long total(int n) const {
+        const int h = (int)(hi - (unsigned)n * FIX_MAGIC_BITS);
+        const int l = (int)(lo - (unsigned)n * FIX_MAGIC_BITS);
+        return ((long long)h << 23) + (long long)l;
     }
 };
 
@@ -242,9 +235,11 @@ __device__ __forceinline__ void lj_f32(const PairF& P, float r2, float& fs, floa
 struct MixedAcc {
     FixAcc ax, ay, az;
     float pe, vr, gmax;
+    int n;
     __device__ __forceinline__ void init() {
         ax.init(); ay.init(); az.init();
         pe = vr = gmax = 0.f;
+        n = 0;
     }
     __device__ __forceinline__ void add(float dx, float dy, float dz, float r2, float fs, float u, float fscale) {
         pe += u;
@@ -254,6 +249,7 @@ struct MixedAcc {
         ax.add(dx * g);
         ay.add(dy * g);
         az.add(dz * g);
+        ++n;
     }
 };
 
@@ -302,21 +298,31 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
             if (SINGLE) P0 = pairf(d.pair[ty * MAX_TYPES + ty]);
             const int n = d.nn[s];
             if (!brute) {
-                // hot loop: FP32 and integer work only
+                // hot loop: FP32 and integer work only, two candidates in flight
                 bool band = false;
-                for (int k = lane; k < n; k += TPA) {
-                    const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
-                    const int j = (int)(e & IDX_MASK);
-                    const float4 xj = __ldg(d.mir + j);
+                auto pair = [&](uint32_t e, float4 xj) {
                     const float4 sh = tab[e >> IDX_BITS];
                     const float dx = xj.x - xi.x + sh.x, dy = xj.y - xi.y + sh.y, dz = xj.z - xi.z + sh.z;
                     const PairF P = SINGLE ? P0 : pairf(d.pair[ty * MAX_TYPES + type_of(xj)]);
                     const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 > P.rc2_hi) continue;
-                    if (r2 >= P.rc2_lo) { band = true; continue; }   // decided in FP64 below
+                    if (r2 > P.rc2_hi) return;
+                    if (r2 >= P.rc2_lo) { band = true; return; }   // decided in FP64 below
                     float fs, u;
                     lj_f32(P, r2, fs, u);
                     acc.add(dx, dy, dz, r2, fs, u, fscale);
+                };
+                int k = lane;
+                for (; k + TPA < n; k += 2 * TPA) {
+                    const uint32_t e0 = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                    const uint32_t e1 = __ldcs(d.nbr + nbr_index(s, k + TPA, TPA, N));
+                    const float4 x0 = __ldg(d.mir + (e0 & IDX_MASK));
+                    const float4 x1 = __ldg(d.mir + (e1 & IDX_MASK));
+                    pair(e0, x0);
+                    pair(e1, x1);
+                }
+                if (k < n) {
+                    const uint32_t e0 = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                    pair(e0, __ldg(d.mir + (e0 & IDX_MASK)));
                 }
                 if (band) {
                     // pairs within 1e-5 of r_cut^2: the reference's FP64 decision
@@ -353,10 +359,11 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
                 }
             }
         }
-        long long sx = acc.ax.total(), sy = acc.ay.total(), sz = acc.az.total();
-        if (act && acc.gmax > split_limit) {
-            // a term may exceed the exact range of the split: redo this lane's
-            // terms with exact float -> int64 conversions (very close pairs only)
+        long long sx = acc.ax.total(acc.n), sy = acc.ay.total(acc.n), sz = acc.az.total(acc.n);
+        if (act && (acc.gmax > split_limit || acc.n > FIX_FOLD)) {
+            // a term may exceed the exact range of the split, or the lane summed
+            // more terms than the 32-bit words hold: redo this lane's terms with
+            // exact float -> int64 conversions (very close pairs, huge lists)
             if (acc.gmax > range_limit) atomicOr(d.err, E_FIXED);
             sx = sy = sz = 0;
             const float4 xi = d.mir[s];

@@ -724,6 +724,7 @@ __device__ void phase_gather(const Dev& d) {
 
 // Verlet neighbour list with skin: every j (of type >= type i, the
 // reference's t1 <= t2 loop, potential.rs:171-172) within rlist of i.
+// Per-atom builder, used for brute-mode replicas (the whole box is one cell).
 __device__ void phase_build_list(const Dev& d) {
     __shared__ int smi[32];
     const int N = d.ntot, cap = d.cap, tpa = d.tpa;
@@ -732,7 +733,7 @@ __device__ void phase_build_list(const Dev& d) {
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
         const RepDev& R = tile_rep(d, tl.x);
-        if (!R.rebuild) continue;
+        if (!R.rebuild || R.mode == MODE_CELLS) continue;  // cell-mode replicas: phase_build_list_cells
         const int s = tl.y + threadIdx.x;
         int cnt = 0;
         if ((int)threadIdx.x < tl.z) {
@@ -811,6 +812,107 @@ __device__ void phase_build_list(const Dev& d) {
     }
 }
 
+// In the reference's order (refmode): ascending (type, index in type), i.e. rank.
+__device__ __forceinline__ void sort_list_by_rank(const Dev& d, int s, int n) {
+    const int N = d.ntot, tpa = d.tpa;
+    for (int a = 1; a < n; ++a) {
+        const uint32_t e = d.nbr[nbr_index(s, a, tpa, N)];
+        const int key = __ldcg(d.rank + (e & IDX_MASK));
+        int k = a - 1;
+        while (k >= 0) {
+            const uint32_t f = d.nbr[nbr_index(s, k, tpa, N)];
+            if (__ldcg(d.rank + (f & IDX_MASK)) <= key) break;
+            d.nbr[nbr_index(s, k + 1, tpa, N)] = f;
+            --k;
+        }
+        d.nbr[nbr_index(s, k + 1, tpa, N)] = e;
+    }
+}
+
+// Cell-mode replicas: one warp per cell.  Each lane owns one atom of the cell
+// (a cell of more than 32 atoms takes several passes); the atoms of the 27
+// neighbour cells are staged through shared memory 32 at a time with
+// coalesced loads and tested by every lane from the broadcast copy, so all
+// lanes walk the same candidate sequence.
+__device__ void phase_build_list_cells(const Dev& d) {
+    __shared__ float4 stage[TILE / 32][32];
+    const int N = d.ntot, cap = d.cap, tpa = d.tpa;
+    const float rl = (float)(d.rlist * (1.0 + 1e-5));
+    const float rl2 = rl * rl;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int c = gw; c < d.ncells; c += nw) {
+        const int r = d.cell_rep[c];
+        const RepDev* W = d.rep + r;
+        if (!__ldcg(&W->rebuild) || __ldcg(&W->mode) != MODE_CELLS) continue;
+        const int nc[3] = {__ldcg(&W->nc[0]), __ldcg(&W->nc[1]), __ldcg(&W->nc[2])};
+        const int base = __ldcg(&W->cell_base);
+        const int local = c - base;
+        if (local >= nc[0] * nc[1] * nc[2]) continue;   // spare cell capacity
+        const long long rbeg = __ldcg(&W->begin);
+        const int rn = __ldcg(&W->n);
+        const float cs[3] = {dbl_to_flt_rn(__ldcg(&W->cs[0])), dbl_to_flt_rn(__ldcg(&W->cs[1])),
+                             dbl_to_flt_rn(__ldcg(&W->cs[2]))};
+        int cx, cy, cz;
+        decode_cell(local, nc, cx, cy, cz);
+        const int ib = __ldcg(d.cell_start + c), in = __ldcg(d.cell_count + c);
+        if (ib < rbeg || ib + in > rbeg + rn) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
+        int cmax = 0;
+        for (int g = 0; g < in; g += 32) {
+            const int s = ib + g + lane;
+            const bool own = g + lane < in;
+            const float4 xi = own ? __ldcg(d.mir + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int ti = own ? type_of(xi) : 0x7FFFFFFF;
+            int cnt = 0;
+            for (int dz = -1; dz <= 1; ++dz) {
+                int z = cz + dz; z = z < 0 ? z + nc[2] : (z >= nc[2] ? z - nc[2] : z);
+                for (int dy = -1; dy <= 1; ++dy) {
+                    int y = cy + dy; y = y < 0 ? y + nc[1] : (y >= nc[1] ? y - nc[1] : y);
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        int x = cx + dx; x = x < 0 ? x + nc[0] : (x >= nc[0] ? x - nc[0] : x);
+                        const int cj = base + (x * nc[1] + y) * nc[2] + z;
+                        const uint32_t code = (uint32_t)((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
+                        const float sx = (float)dx * cs[0], sy = (float)dy * cs[1], sz = (float)dz * cs[2];
+                        const int jb = __ldcg(d.cell_start + cj), jn = __ldcg(d.cell_count + cj);
+                        if (jb < rbeg || jb + jn > rbeg + rn) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
+                        for (int kk = 0; kk < jn; kk += 32) {
+                            const int m = min(32, jn - kk);
+                            __syncwarp();
+                            if (lane < m) stage[wib][lane] = __ldcg(d.mir + jb + kk + lane);
+                            __syncwarp();
+                            for (int k = 0; k < m; ++k) {
+                                const float4 xj = stage[wib][k];
+                                const int j = jb + kk + k;
+                                const float ex = xj.x - xi.x + sx, ey = xj.y - xi.y + sy, ez = xj.z - xi.z + sz;
+                                const bool take = own && j != s && type_of(xj) >= ti &&
+                                                  ex * ex + ey * ey + ez * ez < rl2;
+                                if (take) {
+                                    if (cnt < cap) d.nbr[nbr_index(s, cnt, tpa, N)] = (uint32_t)j | (code << IDX_BITS);
+                                    ++cnt;
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            if (own) {
+                const int n = min(cnt, cap);
+                if (d.refmode) sort_list_by_rank(d, s, n);
+                d.nn[s] = n;
+                if (cnt > cap) {
+                    atomicOr(d.err, E_NLIST);
+                    atomicMax(d.max_needed, cnt);
+                }
+            }
+            cmax = max(cmax, cnt);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_down_sync(0xffffffffu, cmax, off));
+        if (lane == 0 && cmax > 0) atomicMax(&d.rep[r].max_nn, cmax);
+    }
+}
+
 __device__ void phase_rebuild_done(const Dev& d) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int nt = gridDim.x * blockDim.x;
@@ -863,6 +965,7 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
     phase_gather(d);
     grid_barrier(d);
     phase_build_list(d);
+    phase_build_list_cells(d);
     grid_barrier(d);
     phase_rebuild_done(d);
 }
