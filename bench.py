@@ -361,6 +361,229 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Other configurations (each prints its own JSON line; the default line is lj1m)
+
+def _timed_steps(eng, nsteps, dt, **kw):
+    """K steps on the engine's stream, CUDA-event timed; returns ms."""
+    import torch
+    stream = torch.cuda.ExternalStream(eng.stream_ptr)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    if kw.get("ensemble"):
+        eng.ensemble_step(nsteps, dt)
+    else:
+        eng.step(nsteps, dt, **{k: v for k, v in kw.items() if k != "ensemble"})
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b)
+
+
+def run_argon(args):
+    """Argon, 1000 atoms on a 10^3 simple-cubic lattice (edge 3.338339 nm,
+    m = 66.335, sigma = 0.3405 nm, eps/kB = 119.8 K), Maxwell-Boltzmann at
+    273.15 K, Berendsen thermostat tau 10 -> 300 K and barostat (1, 5) ->
+    1.01325, dt 0.002, 1000 steps: the reference's own units."""
+    from moldyn_gb300.engine import Engine
+    from moldyn_gb300.initializer import Barostat, Thermostat, UnitCell, lattice_positions, maxwell_boltzmann
+    a, m, sig, eps = 3.338339, 66.335, 0.3405, 119.8 * K_B * 0.01
+    pos = lattice_positions(UnitCell.U, (10, 10, 10), a)
+    vel = maxwell_boltzmann(1000, 273.15, m, 7)
+    box = np.full(3, 10 * a)
+    n, steps = len(pos), args.steps
+    res = {}
+    for prec, ref in (("fp64", True), ("mixed", False)):
+        e = Engine(precision=prec, reference_order=ref)
+        e.set_potential(0, 0, sig, eps)
+        e.upload(np.zeros(n, dtype=np.uint16), pos, vel, [m], box)
+        e.compute_forces()
+        th, ba = Thermostat.Berendsen(10.0), Barostat.Berendsen(1.0, 5.0)
+        ms = _timed_steps(e, steps, 0.002, thermostat=th, target_temperature=300.0, barostat=ba,
+                          target_pressure=1.01325)
+        out = e.download()
+        mac = e.macro(0)
+        res[prec] = dict(value=n * steps / (ms * 1e-3), ms=ms, out=out, mac=mac, lam=th.lambda_, myu=ba.myu)
+        e.close()
+    # the oracle (reference algorithm) on the same trajectory, timed on the host
+    from oracle import oracle as o
+    st = o.OracleState([n], pos, vel, [m], box, o.pot_table(1, default=(sig, eps)))
+    st.update_force(nthreads=os.cpu_count() or 1)
+    oth, oba = o.Thermostat(o.BERENDSEN, 10.0, 0.0, 0.0), o.Barostat(1.0, 5.0, 0.0)
+    t0 = time.perf_counter()
+    st.step(0.002, nsteps=steps, barostat=oba, P0=1.01325, thermostat=oth, T0=300.0,
+            nthreads=os.cpu_count() or 1)
+    tcpu = time.perf_counter() - t0
+    f64 = res["fp64"]["out"]
+    d = f64["pos"] - st.pos
+    d -= st.box * np.round(d / st.box)
+    line = {"metric": METRIC, "value": res["mixed"]["value"], "unit": "atom-steps/s", "n_gpus": 1,
+            "steps": steps, "higher_is_better": True, "dtype": "f32/i64-fixed/f64",
+            "data": "synthetic: argon U lattice 10^3, seeded Maxwell-Boltzmann 273.15 K",
+            "config": {"workload": "argon_1000_berendsen_TP", "atoms": n, "sigma_nm": sig, "eps": eps,
+                       "mass": m, "dt_ps": 0.002, "thermostat": "Berendsen tau 10 -> 300 K",
+                       "barostat": "Berendsen (1, 5) -> 1.01325",
+                       "fp64_reference_order": {"value": res["fp64"]["value"],
+                                                "max_pos_diff_vs_oracle_nm": float(np.abs(d).max()),
+                                                "box_rel_diff_vs_oracle": float(np.abs(f64["box"] / st.box - 1).max()),
+                                                "lambda": res["fp64"]["lam"], "oracle_lambda": oth.lambda_,
+                                                "myu": res["fp64"]["myu"], "oracle_myu": oba.myu},
+                       "final_T_K": res["mixed"]["mac"]["temperature"], "final_P": res["mixed"]["mac"]["pressure"],
+                       "oracle_final_T_K": st.temperature(0), "oracle_final_P": st.pressure(0)},
+            "cpu_baseline": {"value": n * steps / tcpu, "unit": "atom-steps/s", "cores": os.cpu_count(),
+                             "kind": "port", "sample": f"full run: {steps} steps of the oracle"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_lj8m(args):
+    """8,000,000 atoms: FCC 100x100x200 cells at rho* 0.8442, T* 0.72, Berendsen
+    thermostat tau* 0.5 -> T* 0.72 and barostat (beta 1, tau_P* 5) -> P* 1.0,
+    500 steps; per-kernel roofline."""
+    global CELLS
+    if args.cells == "50,50,100":      # the default cells belong to lj1m
+        CELLS = (100, 100, 200)
+    from moldyn_gb300.engine import Engine
+    from moldyn_gb300.initializer import Barostat, Thermostat
+    pos, vel, box = make_system(seed=88)
+    n = len(pos)
+    T0 = T_STAR * 100.0 / K_B
+    e = Engine(precision="mixed", skin=SKIN, profile=True)
+    e.set_potential(0, 0, 1.0, 1.0)
+    e.upload(np.zeros(n, dtype=np.uint16), pos, vel, [1.0], box)
+    e.compute_forces()
+    th, ba = Thermostat.Berendsen(0.5), Barostat.Berendsen(1.0, 5.0)
+    kw = dict(thermostat=th, target_temperature=T0, barostat=ba, target_pressure=1.0)
+    e.step(args.warmup, DT, **kw)
+    e.reset_stats()
+    with ClockSampler(0) as clk:
+        ms = _timed_steps(e, args.steps, DT, **kw)
+    st = e.stats()
+    mac = e.macro(0)
+    end = e.download()
+    e.close()
+    peak, kind = measured_peaks()
+    f_ms = st.force_ms / max(st.force_launches, 1)
+    p_ms = st.integrate_ms / max(st.integrate_launches, 1)
+    # k_pre algorithmic bytes per atom without a rebuild: pos r/w 64, vel r/w 48,
+    # force read 24, cell 4, mirror write 16, mirror0 read 16, plus two FP64
+    # reduction passes over velocities and temp (2 x 32)
+    pre_bytes = 64 + 48 + 24 + 4 + 16 + 16 + 64
+    line = {"metric": METRIC, "value": n * args.steps / (ms * 1e-3), "unit": "atom-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "dtype": "f32/i64-fixed/f64", "data": "synthetic: FCC 100x100x200, seeded T*=0.72",
+            "config": {"workload": "lj_fcc_8M_berendsen_TP" if n == 8000000 else f"lj_fcc_{n}_berendsen_TP",
+                       "atoms": n, "rebuilds": st.rebuilds,
+                       "threads_per_atom": st.threads_per_atom, "final_T_star": mac["temperature"] * K_B / 100.0,
+                       "final_P_star": mac["pressure"], "final_box": end["box"].tolist()},
+            "clocks": clk.summary(),
+            "kernels": {"k_force_mixed": {"avg_ms": f_ms, "bytes_per_atom": BYTES_PER_ATOM_FORCE,
+                                          "achieved_GBps": BYTES_PER_ATOM_FORCE * n / (f_ms * 1e-3) / 1e9,
+                                          "peak_GBps": peak, "peak_source": kind},
+                        "k_pre": {"avg_ms_incl_rebuilds": p_ms, "bytes_per_atom_no_rebuild": pre_bytes,
+                                  "achieved_GBps": pre_bytes * n / (p_ms * 1e-3) / 1e9, "peak_GBps": peak}}}
+    print(json.dumps(line), flush=True)
+
+
+def make_ensemble(nrep=512, seed=2024):
+    """512 replicas: n^3 atoms on a simple-cubic lattice, n log-uniform in
+    [4, 40]; rho* uniform in [0.01, 0.9]; T* uniform in [0.5, 2.0]; seeded
+    velocities; each replica its own box, Berendsen T target T* and P target
+    near its ideal-gas pressure rho* T*."""
+    from moldyn_gb300.initializer import UnitCell, lattice_positions, maxwell_boltzmann
+    rng = np.random.default_rng(seed)
+    ns = np.rint(np.exp(rng.uniform(np.log(4), np.log(40), nrep))).astype(int)
+    rho = rng.uniform(0.01, 0.9, nrep)
+    tst = rng.uniform(0.5, 2.0, nrep)
+    pos, vel, boxes, offs = [], [], [], [0]
+    for r in range(nrep):
+        a = rho[r] ** (-1.0 / 3.0)
+        p = lattice_positions(UnitCell.U, (ns[r],) * 3, a)
+        pos.append(p)
+        vel.append(maxwell_boltzmann(len(p), tst[r] * 100.0 / K_B, 1.0, seed * 1000 + r))
+        boxes.append(np.full(3, ns[r] * a))
+        offs.append(offs[-1] + len(p))
+    p0 = rho * tst * rng.uniform(0.8, 1.2, nrep)
+    return (np.array(offs), np.concatenate(pos), np.concatenate(vel), np.array(boxes), ns, rho, tst, p0)
+
+
+def run_ensemble(args):
+    from moldyn_gb300.engine import Engine
+    from moldyn_gb300.initializer import Barostat, Thermostat
+    offs, pos, vel, boxes, ns, rho, tst, p0 = make_ensemble()
+    n, nrep = len(pos), len(offs) - 1
+    t0s = tst * 100.0 / K_B
+    res = {}
+    for prec in ("mixed", "fp64"):
+        e = Engine(precision=prec, skin=SKIN, persistent=True, graph_steps=50)
+        e.set_potential(0, 0, 1.0, 1.0)
+        e.upload_ensemble(offs, np.zeros(n, dtype=np.uint16), pos, vel, [1.0], boxes)
+        e.compute_forces()
+        ths = [Thermostat.Berendsen(0.5) for _ in range(nrep)]
+        bas = [Barostat.Berendsen(1.0, 5.0) for _ in range(nrep)]
+        e.ensemble_set_coupling(ths, t0s, bas, p0)
+        steps = args.steps if prec == "mixed" else max(50, min(args.steps, args.fp64_steps))
+        e.ensemble_step(50, DT)            # warm-up, graph capture
+        e.reset_stats()
+        ms = _timed_steps(e, steps, DT, ensemble=True)
+        st = e.stats()
+        res[prec] = {"value": n * steps / (ms * 1e-3), "steps": steps, "ms_per_step": ms / steps,
+                     "graph_launches": st.graph_launches, "rebuilds": st.rebuilds, "tpa": st.threads_per_atom}
+        e.close()
+    line = {"metric": METRIC, "value": res["mixed"]["value"], "unit": "atom-steps/s", "n_gpus": 1,
+            "steps": res["mixed"]["steps"], "higher_is_better": True, "dtype": "f32/i64-fixed/f64",
+            "data": "synthetic: 512 seeded replicas (simple-cubic lattices)",
+            "config": {"workload": "ensemble_512_replicas", "replicas": nrep, "atoms": int(n),
+                       "atoms_min_max_mean": [int(ns.min() ** 3), int(ns.max() ** 3), float((ns ** 3).mean())],
+                       "graph_steps": 50, "persistent_force_kernel": True,
+                       "mixed": res["mixed"], "fp64_plain_path": res["fp64"],
+                       "mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"]}}
+    print(json.dumps(line), flush=True)
+
+
+def run_drift(args):
+    """256,000 atoms (FCC 40^3 cells), NVE at dt* 0.005: total-energy drift of
+    the FP32-naive, mixed (FP32 + fixed point) and FP64 paths."""
+    global CELLS
+    CELLS = (40, 40, 40)
+    from moldyn_gb300.engine import Engine
+    pos, vel, box = make_system(seed=55)
+    n = len(pos)
+    out = {}
+    for prec in ("fp32_naive", "mixed", "fp64"):
+        steps = args.steps if prec != "fp64" else min(args.steps, args.fp64_steps)
+        every = max(1, steps // 100)
+        e = Engine(precision=prec, skin=SKIN)
+        e.set_potential(0, 0, 1.0, 1.0)
+        e.upload(np.zeros(n, dtype=np.uint16), pos, vel, [1.0], box)
+        e.compute_forces()
+        es, ts, ps = [], [], []
+        t0 = time.perf_counter()
+        for k in range(0, steps + 1, every):
+            if k:
+                e.step(every, DT)
+            m = e.macro(0)
+            es.append(m["kinetic_energy"] + m["potential_energy"])
+            ts.append(m["temperature"] * K_B / 100.0)
+            ps.append(m["pressure"])
+        wall = time.perf_counter() - t0
+        es = np.array(es)
+        x = np.arange(len(es)) * every * DT
+        slope = float(np.polyfit(x, es / n, 1)[0]) if len(es) > 2 else 0.0
+        out[prec] = {"steps": steps, "E0_per_atom": float(es[0] / n),
+                     "drift_per_atom_per_tau": slope,
+                     "rel_change": float((es[-1] - es[0]) / abs(es[0])),
+                     "max_rel_dev": float(np.abs(es - es[0]).max() / abs(es[0])),
+                     "T_star_mean": float(np.mean(ts)), "P_star_mean": float(np.mean(ps)),
+                     "wall_s": wall}
+        e.close()
+    line = {"metric": "NVE energy drift (per atom per tau*), 256k LJ atoms", "value": out["mixed"]["drift_per_atom_per_tau"],
+            "unit": "eps/(atom tau)", "higher_is_better": False,
+            "config": {"workload": "drift_256k_nve", "atoms": n, "dt_star": DT, "variants": out,
+                       "mixed_over_fp64_drift": (abs(out["mixed"]["drift_per_atom_per_tau"]) /
+                                                 max(abs(out["fp64"]["drift_per_atom_per_tau"]), 1e-30))}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -373,6 +596,8 @@ def main():
                     help="FCC unit cells (profiling uses smaller boxes; the bench line uses the default)")
     ap.add_argument("--legs", default="all", choices=["all", "mixed"],
                     help="'mixed' runs only the timed mixed leg (for profiler captures)")
+    ap.add_argument("--workload", default="lj1m", choices=["lj1m", "argon", "lj8m", "ensemble", "drift"],
+                    help="lj1m: the headline 1M-atom box (default); the others are the remaining configurations")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -380,8 +605,10 @@ def main():
     CELLS = tuple(int(c) for c in args.cells.split(","))
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.workload == "lj1m":
         run_ours(args)
+    else:
+        {"argon": run_argon, "lj8m": run_lj8m, "ensemble": run_ensemble, "drift": run_drift}[args.workload](args)
 
 
 if __name__ == "__main__":

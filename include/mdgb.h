@@ -82,6 +82,7 @@ extern "C" {
 /* ---- precision ------------------------------------------------------- */
 #define MDGB_PRECISION_FP64 0  /* plain path: the reference's FP64 arithmetic */
 #define MDGB_PRECISION_MIXED 1 /* FP32 pair maths, 64-bit fixed-point force sums, FP64 drift/reductions */
+#define MDGB_PRECISION_FP32_NAIVE 2 /* precision-study variant: as MIXED but force sums in plain FP32 */
 
 /* ---- flags ----------------------------------------------------------- */
 /* FP64 only: reproduce the reference's summation order (neighbour lists in

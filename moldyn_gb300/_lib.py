@@ -25,6 +25,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no state uploaded
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_FP32_NAIVE = 2
 FLAG_REFERENCE_ORDER = 1
 FLAG_PROFILE = 2
 FLAG_PERSISTENT = 4

@@ -33,7 +33,7 @@ __global__ void k_scatter_in(Dev d, const double*, const double*, const int*, co
 __global__ void k_scatter_forces(Dev d, const double*, const double*, const double*);
 __global__ void k_pairs(Dev d, long long capacity, int* out_i, int* out_j, unsigned long long* count);
 using force_fn = void (*)(Dev, StepParams);
-force_fn force_kernel(int tpa, bool mixed, bool single, bool kick, bool persistent);
+force_fn force_kernel(int tpa, int precision, bool single, bool kick, bool persistent);
 }  // namespace mdgb
 
 using namespace mdgb;
@@ -263,7 +263,7 @@ int launch_pre(mdgb_engine* e, const StepParams& sp) {
 
 int launch_force(mdgb_engine* e, const StepParams& sp, bool kick) {
     const bool persistent = (e->cfg.flags & MDGB_FLAG_PERSISTENT) != 0;
-    force_fn fn = force_kernel(e->tpa, e->dev.mixed != 0, e->dev.single_type != 0, kick, persistent);
+    force_fn fn = force_kernel(e->tpa, e->cfg.precision, e->dev.single_type != 0, kick, persistent);
     if (!fn) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "threads_per_atom must be 1, 2, 4 or 8");
     cudaEvent_t pe;
     prof_begin(e, 0, &pe);
@@ -651,11 +651,20 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     }
     e->ntiles = (int)tiles.size();
     e->ncells = (int)cell_rep.size();
+    // reduction chunks: runs of <= CHUNK_TILES tiles inside one replica
+    std::vector<int4> chunks;
+    for (int r = 0; r < nrep; ++r) {
+        RepDev& R = e->rep_host[r];
+        R.chunk_begin = (int)chunks.size();
+        for (int t = 0; t < R.ntiles; t += CHUNK_TILES)
+            chunks.push_back(make_int4(r, R.tile_begin + t, std::min(CHUNK_TILES, R.ntiles - t), 0));
+        R.nchunks = (int)chunks.size() - R.chunk_begin;
+    }
 
     Dev& d = e->dev;
     d.ntot = N; d.ntiles = e->ntiles; d.nrep = nrep; d.ncells = e->ncells;
     d.refmode = (e->cfg.flags & MDGB_FLAG_REFERENCE_ORDER) && e->cfg.precision == MDGB_PRECISION_FP64 ? 1 : 0;
-    d.mixed = e->cfg.precision == MDGB_PRECISION_MIXED ? 1 : 0;
+    d.mixed = e->cfg.precision != MDGB_PRECISION_FP64 ? 1 : 0;
     d.single_type = ntypes == 1 ? 1 : 0;
     d.last_type = ntypes - 1;
     for (int t = 0; t < MAX_TYPES; ++t) d.mass[t] = t < ntypes ? mass_per_type[t] : 1.0;
@@ -666,6 +675,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         (rc = dalloc(e, &d.cell, N)) || (rc = dalloc(e, &d.orig, N)) || (rc = dalloc(e, &d.rank, N)) ||
         (rc = dalloc(e, &d.nn, N)) || (rc = dalloc(e, &d.tiles, e->ntiles)) ||
         (rc = dalloc(e, &d.rep, nrep)) || (rc = dalloc(e, &d.part, 8 * (size_t)e->ntiles)) ||
+        (rc = dalloc(e, &d.cpart, 8 * chunks.size())) || (rc = dalloc(e, &d.chunks, chunks.size())) ||
         (rc = dalloc(e, &d.err, 2)) || (rc = dalloc(e, &d.max_needed, 1)) ||
         (rc = dalloc(e, &d.cell_count, e->ncells)) || (rc = dalloc(e, &d.cell_fill, e->ncells)) ||
         (rc = dalloc(e, &d.cell_start, e->ncells + 1)) || (rc = dalloc(e, &d.cell_rep, e->ncells)) ||
@@ -708,6 +718,8 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
 
     CU(cudaMemcpyAsync(d.tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, e->stream));
+    d.nchunks = (int)chunks.size();
+    CU(cudaMemcpyAsync(d.chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice, e->stream));
     CU(cudaMemcpyAsync(d.tile_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream));
     CU(cudaMemcpyAsync(d.cell_rep, cell_rep.data(), cell_rep.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream));
     CU(cudaMemsetAsync(d.cell_count, 0, e->ncells * sizeof(int), e->stream));
@@ -894,7 +906,9 @@ MDGB_API int mdgb_create(const mdgb_config* cfg, mdgb_engine** out) {
     *out = nullptr;
     mdgb_config c;
     if (cfg) c = *cfg; else mdgb_config_default(&c);
-    if (c.precision != MDGB_PRECISION_FP64 && c.precision != MDGB_PRECISION_MIXED) return MDGB_ERR_INVALID_ARGUMENT;
+    if (c.precision != MDGB_PRECISION_FP64 && c.precision != MDGB_PRECISION_MIXED &&
+        c.precision != MDGB_PRECISION_FP32_NAIVE)
+        return MDGB_ERR_INVALID_ARGUMENT;
     if (c.threads_per_atom != 0 && c.threads_per_atom != 1 && c.threads_per_atom != 2 &&
         c.threads_per_atom != 4 && c.threads_per_atom != 8)
         return MDGB_ERR_INVALID_ARGUMENT;

@@ -232,18 +232,27 @@ __device__ __forceinline__ void lj_f32(const PairF& P, float r2, float& fs, floa
     u = fmaf(P.eps4 * s6, s6 - 1.0f, -P.ucut);
 }
 
+// NAIVE: the FP32-naive variant of the precision study -- force sums in plain
+// FP32 registers instead of fixed point (same pair maths).
+template <bool NAIVE>
 struct MixedAcc {
     FixAcc ax, ay, az;
+    float fx, fy, fz;
     float pe, vr, gmax;
     int n;
     __device__ __forceinline__ void init() {
         ax.init(); ay.init(); az.init();
+        fx = fy = fz = 0.f;
         pe = vr = gmax = 0.f;
         n = 0;
     }
     __device__ __forceinline__ void add(float dx, float dy, float dz, float r2, float fs, float u, float fscale) {
         pe += u;
         vr = fmaf(fs, r2, vr);
+        if (NAIVE) {
+            fx = fmaf(dx, fs, fx); fy = fmaf(dy, fs, fy); fz = fmaf(dz, fs, fz);
+            return;
+        }
         const float g = fs * fscale;
         gmax = fmaxf(gmax, fabsf(g));
         ax.add(dx * g);
@@ -265,7 +274,7 @@ __device__ __forceinline__ bool exact_pair(const Dev& d, const RepDev* R, int s,
     return true;
 }
 
-template <int TPA, bool SINGLE, bool KICK, bool PERSIST>
+template <int TPA, bool SINGLE, bool KICK, bool PERSIST, bool NAIVE = false>
 __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp) {
     __shared__ float4 tab[27];
     __shared__ int s_tile;
@@ -288,7 +297,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
         const bool brute = R->mode == MODE_BRUTE;
         const int s = tl.y + a;
         const bool act = a < tl.z;
-        MixedAcc acc;
+        MixedAcc<NAIVE> acc;
         acc.init();
         int ty = 0;
         if (act) {
@@ -360,7 +369,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
             }
         }
         long long sx = acc.ax.total(acc.n), sy = acc.ay.total(acc.n), sz = acc.az.total(acc.n);
-        if (act && (acc.gmax > split_limit || acc.n > FIX_FOLD)) {
+        if (!NAIVE && act && (acc.gmax > split_limit || acc.n > FIX_FOLD)) {
             // a term may exceed the exact range of the split, or the lane summed
             // more terms than the 32-bit words hold: redo this lane's terms with
             // exact float -> int64 conversions (very close pairs, huge lists)
@@ -393,13 +402,19 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
             }
         }
         float pe = acc.pe, vr = acc.vr;
+        float nfx = acc.fx, nfy = acc.fy, nfz = acc.fz;
         if (TPA > 1) {
-            sx = tpa_sum_ll<TPA>(sx); sy = tpa_sum_ll<TPA>(sy); sz = tpa_sum_ll<TPA>(sz);
+            if (NAIVE) {
+                nfx = tpa_sum_f<TPA>(nfx); nfy = tpa_sum_f<TPA>(nfy); nfz = tpa_sum_f<TPA>(nfz);
+            } else {
+                sx = tpa_sum_ll<TPA>(sx); sy = tpa_sum_ll<TPA>(sy); sz = tpa_sum_ll<TPA>(sz);
+            }
             pe = tpa_sum_f<TPA>(pe); vr = tpa_sum_f<TPA>(vr);
         }
         if (act && lane == 0) {
-            const double fx = fixed_to_double(sx, d.fscale_log2), fy = fixed_to_double(sy, d.fscale_log2),
-                         fz = fixed_to_double(sz, d.fscale_log2);
+            const double fx = NAIVE ? flt_to_dbl(nfx) : fixed_to_double(sx, d.fscale_log2);
+            const double fy = NAIVE ? flt_to_dbl(nfy) : fixed_to_double(sy, d.fscale_log2);
+            const double fz = NAIVE ? flt_to_dbl(nfz) : fixed_to_double(sz, d.fscale_log2);
             d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
             d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr);
             if (KICK) {
@@ -413,35 +428,41 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
 }
 
 // ---------------------------------------------------------------------------
-// Host-side launch table.
+// Host-side launch table.  precision: 0 FP64 plain, 1 mixed, 2 FP32-naive.
 using force_fn = void (*)(Dev, StepParams);
 
 template <int TPA, bool KICK, bool PERSIST>
-static force_fn pick_mixed(bool single) {
+static force_fn pick_mixed(bool single, bool naive) {
+    if (naive)
+        return single ? (force_fn)k_force_mixed<TPA, true, KICK, PERSIST, true>
+                      : (force_fn)k_force_mixed<TPA, false, KICK, PERSIST, true>;
     return single ? (force_fn)k_force_mixed<TPA, true, KICK, PERSIST>
                   : (force_fn)k_force_mixed<TPA, false, KICK, PERSIST>;
 }
 
 template <int TPA, bool PERSIST>
-static force_fn pick_tpa(bool mixed, bool single, bool kick) {
-    if (mixed) return kick ? pick_mixed<TPA, true, PERSIST>(single) : pick_mixed<TPA, false, PERSIST>(single);
+static force_fn pick_tpa(int precision, bool single, bool kick) {
+    if (precision != 0) {
+        const bool naive = precision == 2;
+        return kick ? pick_mixed<TPA, true, PERSIST>(single, naive) : pick_mixed<TPA, false, PERSIST>(single, naive);
+    }
     return kick ? (force_fn)k_force_fp64<TPA, true, PERSIST> : (force_fn)k_force_fp64<TPA, false, PERSIST>;
 }
 
 template <bool PERSIST>
-static force_fn pick_persist(int tpa, bool mixed, bool single, bool kick) {
+static force_fn pick_persist(int tpa, int precision, bool single, bool kick) {
     switch (tpa) {
-        case 1: return pick_tpa<1, PERSIST>(mixed, single, kick);
-        case 2: return pick_tpa<2, PERSIST>(mixed, single, kick);
-        case 4: return pick_tpa<4, PERSIST>(mixed, single, kick);
-        case 8: return pick_tpa<8, PERSIST>(mixed, single, kick);
+        case 1: return pick_tpa<1, PERSIST>(precision, single, kick);
+        case 2: return pick_tpa<2, PERSIST>(precision, single, kick);
+        case 4: return pick_tpa<4, PERSIST>(precision, single, kick);
+        case 8: return pick_tpa<8, PERSIST>(precision, single, kick);
         default: return nullptr;
     }
 }
 
-force_fn force_kernel(int tpa, bool mixed, bool single, bool kick, bool persistent) {
-    return persistent ? pick_persist<true>(tpa, mixed, single, kick)
-                      : pick_persist<false>(tpa, mixed, single, kick);
+force_fn force_kernel(int tpa, int precision, bool single, bool kick, bool persistent) {
+    return persistent ? pick_persist<true>(tpa, precision, single, kick)
+                      : pick_persist<false>(tpa, precision, single, kick);
 }
 
 }  // namespace mdgb

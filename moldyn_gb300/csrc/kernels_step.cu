@@ -138,11 +138,31 @@ __device__ __forceinline__ int block_max_int(int v, int* sm) {
     return v;
 }
 
-// Sum over the tile partials of one replica by one warp (fixed order).
+// Two-level deterministic reduction of tile partials: one warp per chunk of
+// <= CHUNK_TILES tiles (phase_chunk_sums), then one warp per replica over its
+// chunks -- a replica of millions of atoms is summed by many warps in
+// parallel, always in the same order.
+__device__ void phase_chunk_sums(const Dev& d, int nslots) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int c = gw; c < d.nchunks; c += nw) {
+        const int4 ch = d.chunks[c];
+        for (int k = 0; k < nslots; ++k) {
+            double s = 0.0;
+            for (int t = lane; t < ch.z; t += 32) s += __ldcg(d.part + (size_t)(ch.y + t) * 8 + k);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+            if (lane == 0) d.cpart[(size_t)c * 8 + k] = s;
+        }
+    }
+}
+
+// Sum over the chunk partials of one replica by one warp (fixed order).
 __device__ __forceinline__ double warp_sum_tiles(const Dev& d, const RepDev& R, int slot) {
     const int lane = threadIdx.x & 31;
     double s = 0.0;
-    for (int t = lane; t < R.ntiles; t += 32) s += __ldcg(d.part + (size_t)(R.tile_begin + t) * 8 + slot);
+    for (int c = lane; c < R.nchunks; c += 32) s += __ldcg(d.cpart + (size_t)(R.chunk_begin + c) * 8 + slot);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     return __shfl_sync(0xffffffffu, s, 0);
@@ -859,12 +879,18 @@ __device__ void phase_build_list_cells(const Dev& d) {
         const int ib = __ldcg(d.cell_start + c), in = __ldcg(d.cell_count + c);
         if (ib < rbeg || ib + in > rbeg + rn) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
         int cmax = 0;
+        const bool single = d.single_type != 0;
+        const size_t rowstride = (size_t)N * (size_t)tpa;
         for (int g = 0; g < in; g += 32) {
             const int s = ib + g + lane;
             const bool own = g + lane < in;
             const float4 xi = own ? __ldcg(d.mir + s) : make_float4(0.f, 0.f, 0.f, 0.f);
             const int ti = own ? type_of(xi) : 0x7FFFFFFF;
             int cnt = 0;
+            // running output position: entry cnt of atom s lives at
+            // rowp[col], rowp = nbr + (cnt / tpa) * N * tpa + s * tpa, col = cnt % tpa
+            uint32_t* rowp = d.nbr + (size_t)s * (size_t)tpa;
+            int col = 0;
             for (int dz = -1; dz <= 1; ++dz) {
                 int z = cz + dz; z = z < 0 ? z + nc[2] : (z >= nc[2] ? z - nc[2] : z);
                 for (int dy = -1; dy <= 1; ++dy) {
@@ -873,7 +899,10 @@ __device__ void phase_build_list_cells(const Dev& d) {
                         int x = cx + dx; x = x < 0 ? x + nc[0] : (x >= nc[0] ? x - nc[0] : x);
                         const int cj = base + (x * nc[1] + y) * nc[2] + z;
                         const uint32_t code = (uint32_t)((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
-                        const float sx = (float)dx * cs[0], sy = (float)dy * cs[1], sz = (float)dz * cs[2];
+                        // candidate displacement = xj - (xi - shift)
+                        const float bx = xi.x - (float)dx * cs[0], by = xi.y - (float)dy * cs[1],
+                                    bz = xi.z - (float)dz * cs[2];
+                        const uint32_t tag = code << IDX_BITS;
                         const int jb = __ldcg(d.cell_start + cj), jn = __ldcg(d.cell_count + cj);
                         if (jb < rbeg || jb + jn > rbeg + rn) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
                         for (int kk = 0; kk < jn; kk += 32) {
@@ -881,15 +910,17 @@ __device__ void phase_build_list_cells(const Dev& d) {
                             __syncwarp();
                             if (lane < m) stage[wib][lane] = __ldcg(d.mir + jb + kk + lane);
                             __syncwarp();
+#pragma unroll 2
                             for (int k = 0; k < m; ++k) {
                                 const float4 xj = stage[wib][k];
                                 const int j = jb + kk + k;
-                                const float ex = xj.x - xi.x + sx, ey = xj.y - xi.y + sy, ez = xj.z - xi.z + sz;
-                                const bool take = own && j != s && type_of(xj) >= ti &&
+                                const float ex = xj.x - bx, ey = xj.y - by, ez = xj.z - bz;
+                                const bool take = own && j != s && (single || type_of(xj) >= ti) &&
                                                   ex * ex + ey * ey + ez * ez < rl2;
                                 if (take) {
-                                    if (cnt < cap) d.nbr[nbr_index(s, cnt, tpa, N)] = (uint32_t)j | (code << IDX_BITS);
+                                    if (cnt < cap) rowp[col] = (uint32_t)j | tag;
                                     ++cnt;
+                                    if (++col == tpa) { col = 0; rowp += rowstride; }
                                 }
                             }
                         }
@@ -934,9 +965,13 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
         } else {
             phase_partials1(d, sel);
             grid_barrier(d);
+            phase_chunk_sums(d, 8);
+            grid_barrier(d);
             phase_finalize1(d);
             grid_barrier(d);
             phase_partials2(d, sel);
+            grid_barrier(d);
+            phase_chunk_sums(d, 2);
             grid_barrier(d);
             phase_finalize2(d, sp, true);
             grid_barrier(d);
@@ -979,9 +1014,13 @@ __global__ void __launch_bounds__(TILE) k_macro(Dev d, StepParams sp, int sel) {
     }
     phase_partials1(d, sel);
     grid_barrier(d);
+    phase_chunk_sums(d, 8);
+    grid_barrier(d);
     phase_finalize1(d);
     grid_barrier(d);
     phase_partials2(d, sel);
+    grid_barrier(d);
+    phase_chunk_sums(d, 2);
     grid_barrier(d);
     phase_finalize2(d, sp, false);
 }

@@ -33,6 +33,7 @@ constexpr int TILE = 128;
 constexpr int IDX_BITS = 27;
 constexpr uint32_t IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr int CODE_ZERO = 13;  // (0,0,0)
+constexpr int CHUNK_TILES = 256;  // tiles per reduction chunk
 
 // error bits (device word, read by the host after each chunk)
 enum : int {
@@ -59,6 +60,7 @@ struct RepDev {
     // static, set at upload
     long long begin;
     int n, cell_base, cell_cap, tile_begin, ntiles, last_type_count;
+    int chunk_begin, nchunks;     // reduction chunks of <= CHUNK_TILES tiles
     int type_off[MAX_TYPES + 1];  // reference order: type t owns ranks [begin+off[t], begin+off[t+1])
     // geometry (device-updated)
     double box[3];
@@ -118,6 +120,9 @@ struct Dev {
     RepDev* rep;
     const PairDev* pair;  // [MAX_TYPES*MAX_TYPES]
     double* part;      // [ntiles][8] tile partials
+    double* cpart;     // [nchunks][8] chunk partials
+    int4* chunks;      // (replica, first tile, tile count, 0)
+    int nchunks, pad_ch;
     int* err;
     int* max_needed;   // largest neighbour count requested
     // rebuild scratch

@@ -52,8 +52,9 @@ def _f64(a, shape=None):
 class Engine:
     """One libmdgb handle.
 
-    precision: "fp64" (plain path, the reference's arithmetic) or "mixed"
-    (FP32 pair maths, 64-bit fixed-point force sums, FP64 drift/reductions).
+    precision: "fp64" (plain path, the reference's arithmetic), "mixed"
+    (FP32 pair maths, 64-bit fixed-point force sums, FP64 drift/reductions) or
+    "fp32_naive" (the precision study's variant: force sums in plain FP32).
     reference_order: FP64 only -- reproduce the reference's summation order so
     forces and trajectories are bit-identical to its FP64 CPU results.
     """
@@ -65,7 +66,8 @@ class Engine:
         L = load()
         cfg = _lib.Config()
         check(L.mdgb_config_default(C.byref(cfg)))
-        cfg.precision = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
+        cfg.precision = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED,
+                         "fp32_naive": _lib.PRECISION_FP32_NAIVE}[precision]
         cfg.skin = float(skin)
         cfg.rebuild_every = int(rebuild_every)
         cfg.threads_per_atom = int(threads_per_atom)

@@ -428,16 +428,46 @@ def test_mixed_is_deterministic(mdgb):
 @pytest.mark.parametrize("opts", [dict(graph_steps=10), dict(persistent=True)])
 def test_graph_and_persistent_match_eager(mdgb, opts):
     pos, vel, box = gs.fcc((8, 8, 8), jitter=0.04, seed=32)
-    outs = []
+    outs, graph_launches = [], []
     for kw in ({}, opts):
         e = _engine(mdgb, "mixed", threads_per_atom=2, **kw)
         _upload(e, pos, vel, box)
         e.compute_forces()
         e.step(30, 0.005)
         outs.append(e.download())
+        graph_launches.append(e.stats().graph_launches)
         e.close()
     for k in ("pos", "vel", "force"):
         assert np.array_equal(outs[0][k], outs[1][k]), k
+    assert graph_launches[1] > 0 if "graph_steps" in opts else True
+
+
+def test_argon_berendsen_tp_reference_units(mdgb, oracle):
+    """The argon configuration in the reference's units (U lattice 10^3, edge
+    3.338339 nm, m 66.335, sigma 0.3405 nm, eps/kB 119.8 K, Berendsen tau 10 ->
+    300 K, barostat (1, 5) -> 1.01325, dt 0.002): FP64 reference order against
+    the oracle over 200 steps.  Thermostat factors agree bit for bit; the
+    barostat's cbrt may differ by an ulp per step (CUDA vs C library)."""
+    from moldyn_gb300.initializer import Barostat, Thermostat, UnitCell, lattice_positions, maxwell_boltzmann
+    a, m, sig, eps = 3.338339, 66.335, 0.3405, 119.8 * gs.K_B * 0.01
+    pos = lattice_positions(UnitCell.U, (10, 10, 10), a)
+    vel = maxwell_boltzmann(1000, 273.15, m, 7)
+    box = np.full(3, 10 * a)
+    e = _engine(mdgb, "fp64", ref=True)
+    _upload(e, pos, vel, box, mass=m, sigma=sig, eps=eps)
+    e.compute_forces()
+    th, ba = Thermostat.Berendsen(10.0), Barostat.Berendsen(1.0, 5.0)
+    e.step(200, 0.002, thermostat=th, target_temperature=300.0, barostat=ba, target_pressure=1.01325)
+    out = e.download()
+    e.close()
+    ost = _oracle_state(oracle, pos, vel, box, mass=m, sigma=sig, eps=eps)
+    ost.update_force()
+    oth, oba = oracle.Thermostat(oracle.BERENDSEN, 10.0, 0.0, 0.0), oracle.Barostat(1.0, 5.0, 0.0)
+    ost.step(0.002, nsteps=200, barostat=oba, P0=1.01325, thermostat=oth, T0=300.0)
+    assert abs(th.lambda_ - oth.lambda_) <= 1e-14 and abs(ba.myu - oba.myu) <= 1e-14
+    assert np.allclose(out["box"], ost.box, rtol=1e-13, atol=0)
+    assert np.abs(out["pos"] - ost.pos).max() <= 1e-10
+    assert np.abs(out["vel"] - ost.vel).max() <= 1e-10
 
 
 def test_download_preserves_caller_order(mdgb):
