@@ -440,7 +440,7 @@ def run_lj8m(args):
     thermostat tau* 0.5 -> T* 0.72 and barostat (beta 1, tau_P* 5) -> P* 1.0,
     500 steps; per-kernel roofline."""
     global CELLS
-    if args.cells == "50,50,100":      # the default cells belong to lj1m
+    if not args.cells:
         CELLS = (100, 100, 200)
     from moldyn_gb300.engine import Engine
     from moldyn_gb300.initializer import Barostat, Thermostat
@@ -592,8 +592,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp64-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--cells", default="50,50,100",
-                    help="FCC unit cells (profiling uses smaller boxes; the bench line uses the default)")
+    ap.add_argument("--cells", default=None,
+                    help="FCC unit cells (default 50,50,100 for lj1m, 100,100,200 for lj8m; profiling uses smaller boxes)")
     ap.add_argument("--legs", default="all", choices=["all", "mixed"],
                     help="'mixed' runs only the timed mixed leg (for profiler captures)")
     ap.add_argument("--workload", default="lj1m", choices=["lj1m", "argon", "lj8m", "ensemble", "drift"],
@@ -602,7 +602,8 @@ def main():
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     global CELLS
-    CELLS = tuple(int(c) for c in args.cells.split(","))
+    if args.cells:
+        CELLS = tuple(int(c) for c in args.cells.split(","))
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "lj1m":

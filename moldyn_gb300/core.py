@@ -17,6 +17,20 @@ import numpy as np
 K_B = 1.380648528  # core/src/lib.rs:15
 
 
+def fmt_float(x: float) -> str:
+    """Shortest round-trip decimal with Rust's exponent style ("1e-7")."""
+    x = float(x)
+    if x != x:
+        return "NaN"
+    if x in (float("inf"), float("-inf")):
+        return "inf" if x > 0 else "-inf"
+    r = repr(x)
+    if "e" in r:
+        m, e = r.split("e")
+        return f"{m}e{int(e)}"
+    return r
+
+
 class ParticleDatabase:
     """Process-global particle-type table (particles_database.rs:33-146):
     id -> (name, mass in 1e-27 kg, radius in nm)."""
@@ -54,7 +68,7 @@ class ParticleDatabase:
             w = csv.writer(f, lineterminator="\n")
             w.writerow(["id", "name", "mass", "radius"])
             for i, (name, m, r) in cls._data.items():
-                w.writerow([i, name, repr(float(m)), repr(float(r))])
+                w.writerow([i, name, fmt_float(m), fmt_float(r)])
 
     @classmethod
     def load_particles_data(cls, path):

@@ -213,9 +213,10 @@ __device__ __forceinline__ double wrap_ref(double x, double L) {
 }
 
 // ---------------------------------------------------------------------------
-// Tree-order reductions over atoms of type `sel`.
-// Pass 1 slots: 0-2 sum(v*m), 3 sum(1*m), 4 sum(temp), 5 sum(m*(v.v)/2),
-//               6 sum(potential), 7 count.
+// Tree-order reductions over atoms of type `sel` (all of one mass m, so m is
+// factored out of the sums and applied once per replica; halving is exact
+// and applied once too -- fewer FP64-pipe operations per atom).
+// Pass 1 slots: 0-2 sum(v), 3 count, 4 sum(temp), 5 sum(v.v), 6 sum(potential).
 __device__ void phase_partials1(const Dev& d, int sel) {
     __shared__ double sm[8 * 32];
     const int N = d.ntot;
@@ -224,17 +225,14 @@ __device__ void phase_partials1(const Dev& d, int sel) {
         const int s = tl.y + threadIdx.x;
         double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if ((int)threadIdx.x < tl.z) {
-            const double4_32a p = ldcg4(d.pos + s);
-            const int ty = type_of(p);
+            const int ty = (int)__ldcg(reinterpret_cast<const long long*>(d.pos + s) + 3);
             if (ty == sel) {
-                const double m = d.mass[ty];
                 const double vx = __ldcg(d.vel + s), vy = __ldcg(d.vel + N + s),
                              vz = __ldcg(d.vel + 2 * N + s);
-                v[0] = vx * m; v[1] = vy * m; v[2] = vz * m; v[3] = 1.0 * m;
+                v[0] = vx; v[1] = vy; v[2] = vz; v[3] = 1.0;
                 v[4] = __ldcg(d.evir + s);
-                v[5] = m * (vx * vx + vy * vy + vz * vz) / 2.0;
+                v[5] = vx * vx + vy * vy + vz * vz;
                 v[6] = __ldcg(d.epot + s);
-                v[7] = 1.0;
             }
         }
         block_sum<8>(v, sm);
@@ -243,50 +241,46 @@ __device__ void phase_partials1(const Dev& d, int sel) {
     }
 }
 
-// One warp per replica.
-__device__ void phase_finalize1(const Dev& d) {
+// One warp per replica: COM velocity, momentum, kinetic and potential energy
+// (mod.rs:12-34, energy.rs:14-49).
+__device__ void phase_finalize1(const Dev& d, int sel) {
     const int warps = (gridDim.x * blockDim.x) >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const double m = d.mass[sel];
     for (int r = gw; r < d.nrep; r += warps) {
         const RepDev R = load_rep(d.rep + r);
         double S[8];
-        for (int k = 0; k < 8; ++k) S[k] = warp_sum_tiles(d, R, k);
+        for (int k = 0; k < 7; ++k) S[k] = warp_sum_tiles(d, R, k);
         if ((threadIdx.x & 31) == 0) {
             RepDev* W = d.rep + r;
             W->vcm[0] = S[0] / S[3]; W->vcm[1] = S[1] / S[3]; W->vcm[2] = S[2] / S[3];
-            W->mom[0] = S[0]; W->mom[1] = S[1]; W->mom[2] = S[2];
-            W->msum = S[3]; W->virsum = S[4]; W->ke = S[5]; W->pe = S[6] / 2.0;
-            W->count = (long long)S[7];
+            W->mom[0] = S[0] * m; W->mom[1] = S[1] * m; W->mom[2] = S[2] * m;
+            W->msum = S[3] * m; W->virsum = S[4]; W->ke = 0.5 * (m * S[5]); W->pe = S[6] * 0.5;
+            W->count = (long long)S[3];
         }
     }
 }
 
-// Pass 2 slots: 0 sum(m*|v-vcm|^2/2), 1 sum(m dvx dvx + m dvy dvy + m dvz dvz)
+// Pass 2 slot 0: sum(|v - vcm|^2)
 __device__ void phase_partials2(const Dev& d, int sel) {
-    __shared__ double sm[2 * 32];
+    __shared__ double sm[1 * 32];
     const int N = d.ntot;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
         const int s = tl.y + threadIdx.x;
-        double v[2] = {0, 0};
+        double v[1] = {0};
         if ((int)threadIdx.x < tl.z) {
-            const double4_32a p = ldcg4(d.pos + s);
-            const int ty = type_of(p);
+            const int ty = (int)__ldcg(reinterpret_cast<const long long*>(d.pos + s) + 3);
             if (ty == sel) {
                 const double vc0 = __ldcg(&d.rep[tl.x].vcm[0]), vc1 = __ldcg(&d.rep[tl.x].vcm[1]),
                              vc2 = __ldcg(&d.rep[tl.x].vcm[2]);
-                const double m = d.mass[ty];
                 const double dx = __ldcg(d.vel + s) - vc0, dy = __ldcg(d.vel + N + s) - vc1,
                              dz = __ldcg(d.vel + 2 * N + s) - vc2;
-                v[0] = m * (dx * dx + dy * dy + dz * dz) / 2.0;
-                v[1] = m * dx * dx + m * dy * dy + m * dz * dz;
+                v[0] = dx * dx + dy * dy + dz * dz;
             }
         }
-        block_sum<2>(v, sm);
-        if (threadIdx.x == 0) {
-            d.part[(size_t)t * 8 + 0] = v[0];
-            d.part[(size_t)t * 8 + 1] = v[1];
-        }
+        block_sum<1>(v, sm);
+        if (threadIdx.x == 0) d.part[(size_t)t * 8] = v[0];
     }
 }
 
@@ -319,13 +313,14 @@ __device__ __forceinline__ void coupling_factors(RepDev* W, const RepDev& R, dou
 // Finalize pass 2.  coupling: first apply the box part of the pending
 // barostat update (box *= mu once per type, barostat.rs:45), then T, P and
 // the coupling factors.
-__device__ void phase_finalize2(const Dev& d, const StepParams& sp, bool coupling) {
+__device__ void phase_finalize2(const Dev& d, const StepParams& sp, bool coupling, int sel) {
     const int warps = (gridDim.x * blockDim.x) >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     for (int r = gw; r < d.nrep; r += warps) {
         const RepDev R = load_rep(d.rep + r);
-        const double th = warp_sum_tiles(d, R, 0);
-        const double p1 = warp_sum_tiles(d, R, 1);
+        const double sdv = warp_sum_tiles(d, R, 0);
+        const double p1 = d.mass[sel] * sdv;              // sum m |v - vcm|^2 (pressure.rs:13-17)
+        const double th = 0.5 * p1;                        // energy.rs:25-37
         if ((threadIdx.x & 31) == 0) {
             RepDev* W = d.rep + r;
             double box[3] = {R.box[0], R.box[1], R.box[2]};
@@ -965,15 +960,15 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
         } else {
             phase_partials1(d, sel);
             grid_barrier(d);
-            phase_chunk_sums(d, 8);
+            phase_chunk_sums(d, 7);
             grid_barrier(d);
-            phase_finalize1(d);
+            phase_finalize1(d, sel);
             grid_barrier(d);
             phase_partials2(d, sel);
             grid_barrier(d);
-            phase_chunk_sums(d, 2);
+            phase_chunk_sums(d, 1);
             grid_barrier(d);
-            phase_finalize2(d, sp, true);
+            phase_finalize2(d, sp, true, sel);
             grid_barrier(d);
         }
     }
@@ -1014,15 +1009,15 @@ __global__ void __launch_bounds__(TILE) k_macro(Dev d, StepParams sp, int sel) {
     }
     phase_partials1(d, sel);
     grid_barrier(d);
-    phase_chunk_sums(d, 8);
+    phase_chunk_sums(d, 7);
     grid_barrier(d);
-    phase_finalize1(d);
+    phase_finalize1(d, sel);
     grid_barrier(d);
     phase_partials2(d, sel);
     grid_barrier(d);
-    phase_chunk_sums(d, 2);
+    phase_chunk_sums(d, 1);
     grid_barrier(d);
-    phase_finalize2(d, sp, false);
+    phase_finalize2(d, sp, false, sel);
 }
 
 // End of an mdgb_step call: finish the barostat update of the last step
