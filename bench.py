@@ -507,9 +507,24 @@ def make_ensemble(nrep=512, seed=2024):
 
 
 def run_ensemble(args):
+    import torch
     from moldyn_gb300.engine import Engine
     from moldyn_gb300.initializer import Barostat, Thermostat
+    from moldyn_gb300.sharding import max_over_ranks, replica_cost, shard
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     offs, pos, vel, boxes, ns, rho, tst, p0 = make_ensemble()
+    n_all = len(pos)
+    # replicas are independent: each rank integrates its own cost-balanced share
+    mine = shard(replica_cost(ns ** 3, rho, 2.5 + SKIN), world)[rank]
+    sel = np.concatenate([np.arange(offs[r], offs[r + 1]) for r in mine])
+    pos, vel = pos[sel], vel[sel]
+    offs = np.cumsum([0] + [int(offs[r + 1] - offs[r]) for r in mine])
+    boxes, ns, rho, tst, p0 = boxes[mine], ns[mine], rho[mine], tst[mine], p0[mine]
     n, nrep = len(pos), len(offs) - 1
     t0s = tst * 100.0 / K_B
     res = {}
@@ -524,15 +539,20 @@ def run_ensemble(args):
         steps = args.steps if prec == "mixed" else max(50, min(args.steps, args.fp64_steps))
         e.ensemble_step(50, DT)            # warm-up, graph capture
         e.reset_stats()
-        ms = _timed_steps(e, steps, DT, ensemble=True)
+        if dist is not None:
+            dist.barrier()
+        ms = max_over_ranks(_timed_steps(e, steps, DT, ensemble=True), dist, "cuda")
         st = e.stats()
-        res[prec] = {"value": n * steps / (ms * 1e-3), "steps": steps, "ms_per_step": ms / steps,
+        res[prec] = {"value": n_all * steps / (ms * 1e-3), "steps": steps, "ms_per_step": ms / steps,
                      "graph_launches": st.graph_launches, "rebuilds": st.rebuilds, "tpa": st.threads_per_atom}
         e.close()
-    line = {"metric": METRIC, "value": res["mixed"]["value"], "unit": "atom-steps/s", "n_gpus": 1,
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": res["mixed"]["value"], "unit": "atom-steps/s", "n_gpus": world,
             "steps": res["mixed"]["steps"], "higher_is_better": True, "dtype": "f32/i64-fixed/f64",
-            "data": "synthetic: 512 seeded replicas (simple-cubic lattices)",
-            "config": {"workload": "ensemble_512_replicas", "replicas": nrep, "atoms": int(n),
+            "scaling": "strong", "data": "synthetic: 512 seeded replicas (simple-cubic lattices)",
+            "config": {"workload": "ensemble_512_replicas", "replicas": 512, "atoms": int(n_all),
+                       "replicas_on_rank0": nrep,
                        "atoms_min_max_mean": [int(ns.min() ** 3), int(ns.max() ** 3), float((ns ** 3).mean())],
                        "graph_steps": 50, "persistent_force_kernel": True,
                        "mixed": res["mixed"], "fp64_plain_path": res["fp64"],

@@ -11,8 +11,8 @@ flags of `solve` / `solve-macro-parameters` (--precision, --reference-order,
   * --frames-per-save is honoured (the reference parses it and ignores it):
     frame files are written every N steps, numbered by step as before.
   * initialize takes --seed (the reference's velocity draw is unseeded).
-  * unimplemented choices (custom integrator/thermostat/barostat/potential,
-    Nose-Hoover) exit with an error message instead of panicking.
+  * unimplemented choices (custom integrator/thermostat/barostat/potential)
+    exit with an error message instead of panicking.
 """
 from __future__ import annotations
 
@@ -166,13 +166,16 @@ def cmd_solve(args):
     th = ba = None
     t0 = p0 = 0.0
     if args.thermostat is not None:
-        if args.thermostat != "berendsen":
-            _fail(f"thermostat {args.thermostat} is not available in this engine yet")
+        if args.thermostat == "custom":
+            _fail("custom thermostats are not implemented (todo!() in the reference)")
+        name = "Berendsen" if args.thermostat == "berendsen" else "Nose-Hoover"
         if not args.thermostat_params:
-            _fail("No thermostat parameters. Need tau for Berendsen")
+            _fail(f"No thermostat parameters. Need tau for {name}")
         if args.temperature is None:
             _fail("No temperature was passed")
-        th, t0 = Thermostat.Berendsen(args.thermostat_params[0]), args.temperature
+        th = (Thermostat.Berendsen(args.thermostat_params[0]) if args.thermostat == "berendsen"
+              else Thermostat.NoseHoover(args.thermostat_params[0]))
+        t0 = args.temperature
     if args.barostat is not None:
         if args.barostat != "berendsen":
             _fail("custom barostats are not implemented (todo!() in the reference)")

@@ -792,8 +792,11 @@ int set_coupling_impl(mdgb_engine* e, const mdgb_thermostat* th, const mdgb_baro
             R.myu = ba[r].myu;
         }
     }
-    if (any_nh)
-        return fail(e, MDGB_ERR_UNSUPPORTED, "Nose-Hoover coupling is not implemented in this engine yet");
+    if (any_nh && e->ntypes > 1)
+        return fail(e, MDGB_ERR_UNSUPPORTED,
+                    "Nose-Hoover coupling is implemented for single-type systems (the reference's per-type "
+                    "psi accumulation across several types is not)");
+    e->thermo_nh = any_nh;
     e->thermo_on = th != nullptr;
     e->baro_on = ba != nullptr;
     CU(cudaMemcpyAsync(e->dev.rep, e->rep_host.data(), e->nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));

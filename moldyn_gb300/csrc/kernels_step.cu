@@ -338,10 +338,28 @@ __device__ void phase_finalize2(const Dev& d, const StepParams& sp, bool couplin
     }
 }
 
+// thermostat.rs:59-65: psi += psi_dot(T') * dt/2 with T' the temperature
+// after the first kick, before the velocity scaling.
+__device__ __forceinline__ void nh_update_psi(RepDev* W, const RepDev& R, double T, double dt) {
+    if (!R.thermo_on || R.thermo_kind != 1) return;
+    const double psi_dot = -((R.th_T0 / T) - 1.0) / R.th_tau;
+    W->psi = R.psi + psi_dot * (dt / 2.0);
+}
+
+__device__ void phase_finalize_nh(const Dev& d, const StepParams& sp, int sel) {
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int r = gw; r < d.nrep; r += warps) {
+        const RepDev R = load_rep(d.rep + r);
+        const double sdv = warp_sum_tiles(d, R, 0);
+        if ((threadIdx.x & 31) == 0) nh_update_psi(d.rep + r, R, temperature_of(0.5 * (d.mass[sel] * sdv), R.count), sp.dt);
+    }
+}
+
 // Reference-order reductions: one thread per replica walks the atoms of type
 // `sel` in the reference's order and sums serially, exactly as the iterator
 // folds of macro_parameters/*.rs do.
-__device__ void phase_serial(const Dev& d, const StepParams& sp, int sel, bool coupling) {
+__device__ void phase_serial(const Dev& d, const StepParams& sp, int sel, bool coupling, bool nh_after_kick = false) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int nt = gridDim.x * blockDim.x;
     const int N = d.ntot;
@@ -370,6 +388,10 @@ __device__ void phase_serial(const Dev& d, const StepParams& sp, int sel, bool c
             r1 += m * dx * dx; r1 += m * dy * dy; r1 += m * dz * dz;   // pressure.rs:13-18
             r2 -= __ldcg(d.evir + s);
         }
+        if (nh_after_kick) {
+            nh_update_psi(W, R, temperature_of(th, e - b), sp.dt);
+            continue;
+        }
         double box[3] = {R.box[0], R.box[1], R.box[2]};
         if (coupling && R.pending != 1.0) {
             for (int k = 0; k < d.ntypes; ++k)
@@ -389,7 +411,23 @@ __device__ void phase_serial(const Dev& d, const StepParams& sp, int sel, bool c
 
 // ---------------------------------------------------------------------------
 // Drift: integrator.rs:30-47 for every atom; mirror + displacement.
-__device__ void phase_drift(const Dev& d, const StepParams& sp) {
+// Nose-Hoover steps: the first kick alone (integrator.rs:30-36), so the
+// thermostat can read the temperature between kick and scaling
+// (thermostat.rs:47-52,59-65).
+__device__ void phase_kick(const Dev& d, const StepParams& sp) {
+    const int N = d.ntot;
+    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
+        const int4 tl = d.tiles[t];
+        const int s = tl.y + threadIdx.x;
+        if ((int)threadIdx.x >= tl.z) continue;
+        const int ty = (int)reinterpret_cast<const long long*>(d.pos + s)[3];
+        const double c = sp.kick_c[ty];
+        for (int a = 0; a < 3; ++a)
+            d.vel[(size_t)a * N + s] = __dadd_rn(d.vel[(size_t)a * N + s], __dmul_rn(d.frc[(size_t)a * N + s], c));
+    }
+}
+
+__device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
     __shared__ float smx[32];
     __shared__ float tc[7];   // box (FP32), half box, scale since the last rebuild
     const int N = d.ntot;
@@ -411,10 +449,15 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp) {
             if (sp.do_drift) {
                 const int ty = type_of(p);
                 const double c = sp.kick_c[ty];
-                double vx = d.vel[s], vy = d.vel[N + s], vz = d.vel[2 * N + s];
-                vx = __dadd_rn(vx, __dmul_rn(d.frc[s], c));             // :30-36 kick
-                vy = __dadd_rn(vy, __dmul_rn(d.frc[N + s], c));
-                vz = __dadd_rn(vz, __dmul_rn(d.frc[2 * N + s], c));
+                double vx, vy, vz;
+                if (kicked) {
+                    vx = __ldcg(d.vel + s); vy = __ldcg(d.vel + N + s); vz = __ldcg(d.vel + 2 * N + s);
+                } else {
+                    vx = d.vel[s]; vy = d.vel[N + s]; vz = d.vel[2 * N + s];
+                    vx = __dadd_rn(vx, __dmul_rn(d.frc[s], c));         // :30-36 kick
+                    vy = __dadd_rn(vy, __dmul_rn(d.frc[N + s], c));
+                    vz = __dadd_rn(vz, __dmul_rn(d.frc[2 * N + s], c));
+                }
                 if (R.thermo_on) {                                       // thermostat.rs:54-58
                     vx = __dmul_rn(vx, R.lambda); vy = __dmul_rn(vy, R.lambda);
                     vz = __dmul_rn(vz, R.lambda);
@@ -972,7 +1015,31 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
             grid_barrier(d);
         }
     }
-    phase_drift(d, sp);
+    if (sp.do_drift && sp.thermo_nh) {
+        const int sel = d.last_type;
+        phase_kick(d, sp);
+        grid_barrier(d);
+        if (d.refmode) {
+            phase_serial(d, sp, sel, false, true);
+            grid_barrier(d);
+        } else {
+            phase_partials1(d, sel);
+            grid_barrier(d);
+            phase_chunk_sums(d, 7);
+            grid_barrier(d);
+            phase_finalize1(d, sel);
+            grid_barrier(d);
+            phase_partials2(d, sel);
+            grid_barrier(d);
+            phase_chunk_sums(d, 1);
+            grid_barrier(d);
+            phase_finalize_nh(d, sp, sel);
+            grid_barrier(d);
+        }
+        phase_drift(d, sp, true);
+    } else {
+        phase_drift(d, sp, false);
+    }
     grid_barrier(d);
     phase_decide(d, sp);
     grid_barrier(d);

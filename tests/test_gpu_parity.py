@@ -272,6 +272,34 @@ def test_berendsen_thermostat_reference_order_bitexact(mdgb, oracle):
     e.close()
 
 
+@pytest.mark.parametrize("ref", [True, False])
+def test_nose_hoover_trajectory(mdgb, oracle, ref):
+    """Nose-Hoover (thermostat.rs:35-39,59-65): psi advances with the
+    temperature before the first kick and again with the temperature between
+    kick and scaling.  lambda = exp(.) uses CUDA's exp against the C library's
+    (they may differ by an ulp), so the bar is 1e-10 after 40 steps."""
+    from moldyn_gb300.initializer import Thermostat
+    pos, vel, box = gs.fcc((5, 5, 5), jitter=0.03, seed=17, t_star=1.1)
+    ost = _oracle_state(oracle, pos, vel, box)
+    ost.update_force()
+    e = _engine(mdgb, "fp64", ref=ref)
+    _upload(e, pos, vel, box)
+    e.compute_forces()
+    th = Thermostat.NoseHoover(0.4)
+    oth = oracle.Thermostat(oracle.NOSE_HOOVER, 0.4, 0.0, 0.0)
+    T0 = gs.t_ref(0.72)
+    for chunk in (1, 39):
+        e.step(chunk, 0.005, thermostat=th, target_temperature=T0)
+        ost.step(0.005, nsteps=chunk, thermostat=oth, T0=T0)
+        out = e.download()
+        assert abs(th.psi - oth.psi) <= 1e-12 * max(1.0, abs(oth.psi))
+        assert abs(th.lambda_ - oth.lambda_) <= 1e-14
+        assert np.abs(out["pos"] - ost.pos).max() <= 1e-10
+        assert np.abs(out["vel"] - ost.vel).max() <= 1e-10
+    assert oth.psi != 0.0
+    e.close()
+
+
 def test_berendsen_barostat_trajectory(mdgb, oracle):
     """Barostat: mu = cbrt(.) uses CUDA's cbrt against the C library's, so a
     1-ulp difference per step is allowed; trajectories agree to 1e-11."""
