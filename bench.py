@@ -544,7 +544,11 @@ def run_ensemble(args):
         ms = max_over_ranks(_timed_steps(e, steps, DT, ensemble=True), dist, "cuda")
         st = e.stats()
         res[prec] = {"value": n_all * steps / (ms * 1e-3), "steps": steps, "ms_per_step": ms / steps,
-                     "graph_launches": st.graph_launches, "rebuilds": st.rebuilds, "tpa": st.threads_per_atom}
+                     "graph_launches": st.graph_launches, "rebuilds": st.rebuilds,
+                     "threads_per_atom_by_size_class": {"<2048": st.class_threads_per_atom[0],
+                                                        "2048-32767": st.class_threads_per_atom[1],
+                                                        ">=32768": st.class_threads_per_atom[2]},
+                     "replicas_by_size_class": list(st.class_replicas)}
         e.close()
     if rank != 0:
         return

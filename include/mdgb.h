@@ -153,6 +153,8 @@ typedef struct {
     int64_t force_launches;
     double integrate_ms;        /* summed integrate/rebuild-kernel time */
     int64_t integrate_launches;
+    int class_threads_per_atom[3]; /* autotuned per replica size class: <2048, <32768, larger */
+    int class_replicas[3];
 } mdgb_stats;
 
 /* ---- lifecycle ------------------------------------------------------- */

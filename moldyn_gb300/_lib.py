@@ -67,7 +67,8 @@ class CStats(C.Structure):
                 ("graph_launches", C.c_int64), ("neighbor_capacity", C.c_int),
                 ("max_neighbors", C.c_int), ("threads_per_atom", C.c_int), ("retries", C.c_int),
                 ("force_ms", C.c_double), ("force_launches", C.c_int64),
-                ("integrate_ms", C.c_double), ("integrate_launches", C.c_int64)]
+                ("integrate_ms", C.c_double), ("integrate_launches", C.c_int64),
+                ("class_threads_per_atom", C.c_int * 3), ("class_replicas", C.c_int * 3)]
 
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")

@@ -76,8 +76,15 @@ struct mdgb_engine {
     std::vector<RepDev> rep_host;
     double rlist = 0, rcmax = 0, skin = 0;
     int cap = 0;
-    int tpa = 1;
+    int tpa = 1;                     // default / single-class threads per atom
     bool tuned = false;
+    // size classes of replicas (by atom count): their tiles, threads per atom
+    static constexpr int NCLASS = 3;
+    std::vector<int> class_of;       // per replica
+    int class_tpa[NCLASS] = {1, 1, 1};
+    int class_ntiles[NCLASS] = {0, 0, 0};
+    int class_tile_off[NCLASS] = {0, 0, 0};   // offset into dev.tile_order
+    int class_nrep[NCLASS] = {0, 0, 0};
 
     Dev dev{};
     // allocations
@@ -261,23 +268,50 @@ int launch_pre(mdgb_engine* e, const StepParams& sp) {
     return MDGB_OK;
 }
 
-int launch_force(mdgb_engine* e, const StepParams& sp, bool kick) {
+// One force launch per non-empty size class, each with that class's threads
+// per atom (the replicas of a class were listed with the same layout).
+int launch_force_class(mdgb_engine* e, const StepParams& sp, bool kick, int c) {
     const bool persistent = (e->cfg.flags & MDGB_FLAG_PERSISTENT) != 0;
-    force_fn fn = force_kernel(e->tpa, e->cfg.precision, e->dev.single_type != 0, kick, persistent);
+    const int tpa = e->class_tpa[c];
+    force_fn fn = force_kernel(tpa, e->cfg.precision, e->dev.single_type != 0, kick, persistent);
     if (!fn) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "threads_per_atom must be 1, 2, 4 or 8");
+    Dev d = e->dev;
+    d.tile_list = e->dev.tile_order + e->class_tile_off[c];
+    d.ntile_list = e->class_ntiles[c];
+    d.list_class = c;
+    int grid = d.ntile_list;
+    if (persistent) {
+        int bps = 0;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)fn, TILE * tpa, 0));
+        grid = std::min(d.ntile_list, std::max(1, bps) * e->num_sms);
+    }
+    void* args[] = {(void*)&d, (void*)&sp};
+    CU(cudaLaunchKernel((const void*)fn, dim3(grid), dim3(TILE * tpa), args, 0, e->stream));
+    e->st.kernel_launches++;
+    return MDGB_OK;
+}
+
+int launch_force(mdgb_engine* e, const StepParams& sp, bool kick) {
     cudaEvent_t pe;
     prof_begin(e, 0, &pe);
-    int grid = e->ntiles;
-    if (persistent) {
-        CU(cudaMemsetAsync(e->dev.queue, 0, sizeof(unsigned int), e->stream));
-        int bps = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)fn, TILE * e->tpa, 0));
-        grid = std::min(e->ntiles, std::max(1, bps) * e->num_sms);
+    if (e->cfg.flags & MDGB_FLAG_PERSISTENT)
+        CU(cudaMemsetAsync(e->dev.queue, 0, mdgb_engine::NCLASS * sizeof(unsigned int), e->stream));
+    for (int c = 0; c < mdgb_engine::NCLASS; ++c) {
+        if (!e->class_ntiles[c]) continue;
+        int rc = launch_force_class(e, sp, kick, c);
+        if (rc) return rc;
     }
-    void* args[] = {(void*)&e->dev, (void*)&sp};
-    CU(cudaLaunchKernel((const void*)fn, dim3(grid), dim3(TILE * e->tpa), args, 0, e->stream));
     prof_end(e, pe);
-    e->st.kernel_launches++;
+    return MDGB_OK;
+}
+
+// Write the per-replica threads per atom (the list layout) of every size class.
+int apply_class_tpa(mdgb_engine* e) {
+    CU(cudaMemcpyAsync(e->rep_host.data(), e->dev.rep, e->nrep * sizeof(RepDev), cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    for (int r = 0; r < e->nrep; ++r) e->rep_host[r].tpa = e->class_tpa[e->class_of[r]];
+    CU(cudaMemcpyAsync(e->dev.rep, e->rep_host.data(), e->nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
+    e->graph_valid = false;
     return MDGB_OK;
 }
 
@@ -495,13 +529,19 @@ int step_impl(mdgb_engine* e, int64_t nsteps, double dt) {
     return MDGB_OK;
 }
 
+// Threads per atom for each size class: every candidate is timed on every
+// class at once (each class's launch bracketed by its own events), and each
+// class keeps its fastest.
 int autotune_tpa(mdgb_engine* e) {
     e->tuned = true;
-    if (e->dev.refmode) { e->tpa = 1; e->dev.tpa = 1; return refresh(e, true); }
-    if (e->cfg.threads_per_atom > 0) {
-        e->tpa = e->cfg.threads_per_atom;
-        e->dev.tpa = e->tpa;
-        return MDGB_OK;
+    const int NC = mdgb_engine::NCLASS;
+    if (e->dev.refmode || e->cfg.threads_per_atom > 0) {
+        const int t = e->dev.refmode ? 1 : e->cfg.threads_per_atom;
+        for (int c = 0; c < NC; ++c) e->class_tpa[c] = t;
+        e->tpa = t;
+        int rc = apply_class_tpa(e);
+        if (rc) return rc;
+        return refresh(e, true);
     }
     // Keep the caller's forces: tuning evaluates forces into scratch.
     const size_t N = e->ntot;
@@ -509,55 +549,62 @@ int autotune_tpa(mdgb_engine* e) {
     CU(cudaMemcpyAsync(e->snap_d + 3 * N, e->dev.epot, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     CU(cudaMemcpyAsync(e->snap_d + 4 * N, e->dev.evir, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     const int cands[4] = {1, 2, 4, 8};
-    float best = 1e30f;
-    int best_tpa = 1;
-    cudaEvent_t a, b;
-    CU(cudaEventCreate(&a));
-    CU(cudaEventCreate(&b));
+    float best[NC];
+    int best_tpa[NC];
+    for (int c = 0; c < NC; ++c) { best[c] = 1e30f; best_tpa[c] = 1; }
+    cudaEvent_t ev[NC][2];
+    for (int c = 0; c < NC; ++c) { CU(cudaEventCreate(&ev[c][0])); CU(cudaEventCreate(&ev[c][1])); }
     const unsigned saved_flags = e->cfg.flags;
-    e->cfg.flags &= ~MDGB_FLAG_PROFILE;
+    e->cfg.flags &= ~(MDGB_FLAG_PROFILE | MDGB_FLAG_PERSISTENT);
     StepParams sp = make_sp(e, 0.0, false);
-    for (int c : cands) {
-        if (e->ntot < 4096 && c > 1) break;  // tiny systems: not worth measuring
-        e->tpa = c;
-        e->dev.tpa = c;
-        int rc = clear_err(e);
+    int rc = MDGB_OK;
+    for (int ci = 0; ci < 4 && !rc; ++ci) {
+        const int cand = cands[ci];
+        if (e->ntot < 4096 && cand > 1) break;  // tiny systems: not worth measuring
+        for (int c = 0; c < NC; ++c) e->class_tpa[c] = cand;
+        rc = apply_class_tpa(e);
+        if (!rc) rc = clear_err(e);
         if (!rc) rc = refresh(e, true);
         if (!rc) rc = launch_force(e, sp, false);  // warm-up
-        if (rc) { e->cfg.flags = saved_flags; return rc; }
-        CU(cudaEventRecord(a, e->stream));
-        for (int i = 0; i < 3; ++i) {
-            rc = launch_force(e, sp, false);
-            if (rc) { e->cfg.flags = saved_flags; return rc; }
+        if (rc) break;
+        for (int c = 0; c < NC && !rc; ++c) {
+            if (!e->class_ntiles[c]) continue;
+            CU(cudaEventRecord(ev[c][0], e->stream));
+            for (int i = 0; i < 3 && !rc; ++i) rc = launch_force_class(e, sp, false, c);
+            CU(cudaEventRecord(ev[c][1], e->stream));
         }
-        CU(cudaEventRecord(b, e->stream));
-        CU(cudaEventSynchronize(b));
+        if (rc) break;
         int flags = 0;
         rc = read_err(e, &flags);
-        if (rc) { e->cfg.flags = saved_flags; return rc; }
+        if (rc) break;
         if (flags & E_NLIST) {
             rc = grow_list(e);
-            if (rc) { e->cfg.flags = saved_flags; return rc; }
-            rc = clear_err(e);
-            if (rc) { e->cfg.flags = saved_flags; return rc; }
+            if (!rc) rc = clear_err(e);
+            --ci;  // same candidate again with the larger list
             continue;
         }
-        float ms = 0.f;
-        CU(cudaEventElapsedTime(&ms, a, b));
-        if (ms < best) { best = ms; best_tpa = c; }
+        for (int c = 0; c < NC; ++c) {
+            if (!e->class_ntiles[c]) continue;
+            float ms = 0.f;
+            CU(cudaEventElapsedTime(&ms, ev[c][0], ev[c][1]));
+            if (ms < best[c]) { best[c] = ms; best_tpa[c] = cand; }
+        }
     }
     e->cfg.flags = saved_flags;
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    e->tpa = best_tpa;
-    e->dev.tpa = best_tpa;
-    e->st.threads_per_atom = best_tpa;
+    for (int c = 0; c < NC; ++c) { cudaEventDestroy(ev[c][0]); cudaEventDestroy(ev[c][1]); }
+    if (rc) return rc;
+    for (int c = 0; c < NC; ++c) e->class_tpa[c] = best_tpa[c];
+    e->tpa = best_tpa[0];
+    for (int c = NC - 1; c >= 0; --c)
+        if (e->class_ntiles[c]) { e->tpa = best_tpa[c]; break; }
+    e->st.threads_per_atom = e->tpa;
     CU(cudaMemcpyAsync(e->dev.frc, e->snap_d, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     CU(cudaMemcpyAsync(e->dev.epot, e->snap_d + 3 * N, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     CU(cudaMemcpyAsync(e->dev.evir, e->snap_d + 4 * N, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
-    int rc = clear_err(e);
+    rc = apply_class_tpa(e);
+    if (!rc) rc = clear_err(e);
     if (rc) return rc;
-    return refresh(e, true);  // lists in the chosen layout
+    return refresh(e, true);  // lists in the chosen layouts
 }
 
 int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t* type, const double* pos,
@@ -682,7 +729,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         (rc = dalloc(e, &d.perm, N)) || (rc = dalloc(e, &d.tmp_pos, N)) ||
         (rc = dalloc(e, &d.tmp_d, 8 * (size_t)N)) || (rc = dalloc(e, &d.tmp_i, 3 * (size_t)N)) ||
         (rc = dalloc(e, &d.slot_of_rank, N)) || (rc = dalloc(e, &d.bsum, 4096)) ||
-        (rc = dalloc(e, &d.bar, 4)) || (rc = dalloc(e, &d.queue, 1)) ||
+        (rc = dalloc(e, &d.bar, 4)) || (rc = dalloc(e, &d.queue, mdgb_engine::NCLASS)) ||
         (rc = dalloc(e, &d.tile_order, e->ntiles)) ||
         (rc = dalloc(e, &e->snap_pos, N)) || (rc = dalloc(e, &e->snap_d, 8 * (size_t)N)) ||
         (rc = dalloc(e, &e->snap_i, 4 * (size_t)N)) || (rc = dalloc(e, &e->snap_mir0, N)) ||
@@ -715,7 +762,24 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         const double dens = R.n / vol;
         cost[i] = tiles[i].z * std::min((double)R.n, 1.0 + dens * 4.0 / 3.0 * M_PI * std::pow(e->rlist, 3));
     }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    // size classes by replica atom count; tile_order = class 0 tiles, class 1, class 2
+    e->class_of.assign(nrep, 0);
+    for (int c = 0; c < mdgb_engine::NCLASS; ++c) { e->class_ntiles[c] = 0; e->class_nrep[c] = 0; }
+    for (int r = 0; r < nrep; ++r) {
+        const int nr = e->rep_host[r].n;
+        const int c = nr < 2048 ? 0 : (nr < 32768 ? 1 : 2);
+        e->class_of[r] = c;
+        e->rep_host[r].size_class = c;
+        e->class_nrep[c]++;
+        e->class_ntiles[c] += e->rep_host[r].ntiles;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const int ca = e->class_of[tiles[a].x], cb = e->class_of[tiles[b].x];
+        if (ca != cb) return ca < cb;
+        return cost[a] > cost[b];
+    });
+    e->class_tile_off[0] = 0;
+    for (int c = 1; c < mdgb_engine::NCLASS; ++c) e->class_tile_off[c] = e->class_tile_off[c - 1] + e->class_ntiles[c - 1];
 
     CU(cudaMemcpyAsync(d.tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, e->stream));
     d.nchunks = (int)chunks.size();
@@ -726,6 +790,12 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     CU(cudaMemsetAsync(d.max_needed, 0, sizeof(int), e->stream));
     CU(cudaMemsetAsync(d.err, 0, 2 * sizeof(int), e->stream));
     CU(cudaMemsetAsync(d.bar, 0, 4 * sizeof(unsigned int), e->stream));
+    {
+        const int t0 = (e->cfg.flags & MDGB_FLAG_REFERENCE_ORDER) && e->cfg.precision == MDGB_PRECISION_FP64
+                           ? 1 : (e->cfg.threads_per_atom > 0 ? e->cfg.threads_per_atom : 1);
+        for (int c = 0; c < mdgb_engine::NCLASS; ++c) e->class_tpa[c] = t0;
+        for (int r = 0; r < nrep; ++r) e->rep_host[r].tpa = t0;
+    }
     CU(cudaMemcpyAsync(d.rep, e->rep_host.data(), nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
     // staging copies of the caller's arrays
     double* dpos = e->d_out;
@@ -748,7 +818,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     e->forces_valid = false;
     e->thermo_on = e->baro_on = e->thermo_nh = false;
     e->tuned = false;
-    e->tpa = e->cfg.threads_per_atom > 0 ? e->cfg.threads_per_atom : 1;
+    e->tpa = e->class_tpa[0];
     d.tpa = e->tpa;
     // bin and build lists now, so a bare mdgb_step starts from a valid list
     rc = clear_err(e);
@@ -1168,6 +1238,10 @@ MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out) {
     }
     e->st.neighbor_capacity = e->cap;
     e->st.threads_per_atom = e->tpa;
+    for (int c = 0; c < mdgb_engine::NCLASS; ++c) {
+        e->st.class_threads_per_atom[c] = e->class_tpa[c];
+        e->st.class_replicas[c] = e->class_nrep[c];
+    }
     *out = e->st;
     return MDGB_OK;
 }

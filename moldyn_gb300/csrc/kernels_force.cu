@@ -119,14 +119,16 @@ __device__ __forceinline__ float tpa_sum_f(float v) {
     return v;
 }
 
+// The next tile of this launch's tile list: one per block, or (persistent)
+// from a work counter over the list, costliest tiles first.
 __device__ __forceinline__ int next_tile(const Dev& d, bool persistent, int& iter, int* s_tile) {
-    if (!persistent) return (iter++ == 0) ? (int)blockIdx.x : -1;
+    if (!persistent) return (iter++ == 0 && (int)blockIdx.x < d.ntile_list) ? d.tile_list[blockIdx.x] : -1;
     __syncthreads();
-    if (threadIdx.x == 0) *s_tile = (int)atomicAdd(d.queue, 1u);
+    if (threadIdx.x == 0) *s_tile = (int)atomicAdd(d.queue + d.list_class, 1u);
     __syncthreads();
     const int q = *s_tile;
-    if (q >= d.ntiles) return -1;
-    return d.tile_order[q];
+    if (q >= d.ntile_list) return -1;
+    return d.tile_list[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -142,6 +144,8 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
         if (t < 0) return;
         const int4 tl = d.tiles[t];
         const RepDev* R = d.rep + tl.x;
+        const long long rbeg = R->begin;
+        const int rn = R->n;
         __syncthreads();
         shift_table(tab, R);
         __syncthreads();
@@ -158,7 +162,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
             ty = type_of(pi);
             const int n = d.nn[s];
             for (int k = lane; k < n; k += TPA) {
-                const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                const uint32_t e = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
                 const int j = (int)(e & IDX_MASK);
                 const PairDev& P = d.pair[ty * MAX_TYPES + type_of(__ldg(d.mir + j))];
                 // FP32 prefilter (certainly outside r_cut -> skip)
@@ -291,6 +295,8 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
         if (t < 0) return;
         const int4 tl = d.tiles[t];
         const RepDev* R = d.rep + tl.x;
+        const long long rbeg = R->begin;
+        const int rn = R->n;
         __syncthreads();
         shift_table(tab, R);
         __syncthreads();
@@ -322,21 +328,21 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
                 };
                 int k = lane;
                 for (; k + TPA < n; k += 2 * TPA) {
-                    const uint32_t e0 = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
-                    const uint32_t e1 = __ldcs(d.nbr + nbr_index(s, k + TPA, TPA, N));
+                    const uint32_t e0 = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
+                    const uint32_t e1 = __ldcs(d.nbr + list_index(s, k + TPA, TPA, rbeg, rn, d.cap));
                     const float4 x0 = __ldg(d.mir + (e0 & IDX_MASK));
                     const float4 x1 = __ldg(d.mir + (e1 & IDX_MASK));
                     pair(e0, x0);
                     pair(e1, x1);
                 }
                 if (k < n) {
-                    const uint32_t e0 = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                    const uint32_t e0 = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
                     pair(e0, __ldg(d.mir + (e0 & IDX_MASK)));
                 }
                 if (band) {
                     // pairs within 1e-5 of r_cut^2: the reference's FP64 decision
                     for (int k = lane; k < n; k += TPA) {
-                        const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                        const uint32_t e = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
                         const int j = (int)(e & IDX_MASK);
                         const float4 xj = __ldg(d.mir + j);
                         const float4 sh = tab[e >> IDX_BITS];
@@ -356,7 +362,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
                 // brute mode (a box smaller than three list radii): the reference's
                 // FP64 displacement for every pair -- these replicas are tiny
                 for (int k = lane; k < n; k += TPA) {
-                    const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                    const uint32_t e = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
                     const int j = (int)(e & IDX_MASK);
                     const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(__ldg(d.mir + j))];
                     float dx, dy, dz;
@@ -378,7 +384,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
             const float4 xi = d.mir[s];
             const int n = d.nn[s];
             for (int k = lane; k < n; k += TPA) {
-                const uint32_t e = __ldcs(d.nbr + nbr_index(s, k, TPA, N));
+                const uint32_t e = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
                 const int j = (int)(e & IDX_MASK);
                 const float4 xj = __ldg(d.mir + j);
                 const float4 sh = tab[e >> IDX_BITS];

@@ -780,12 +780,29 @@ __device__ void phase_gather(const Dev& d) {
     }
 }
 
+// In the reference's order (refmode): ascending (type, index in type), i.e. rank.
+__device__ __forceinline__ void sort_list_by_rank(const Dev& d, int s, int n, int tpa, long long begin, int nr) {
+    const int cap = d.cap;
+    for (int a = 1; a < n; ++a) {
+        const uint32_t e = d.nbr[list_index(s, a, tpa, begin, nr, cap)];
+        const int key = __ldcg(d.rank + (e & IDX_MASK));
+        int k = a - 1;
+        while (k >= 0) {
+            const uint32_t f = d.nbr[list_index(s, k, tpa, begin, nr, cap)];
+            if (__ldcg(d.rank + (f & IDX_MASK)) <= key) break;
+            d.nbr[list_index(s, k + 1, tpa, begin, nr, cap)] = f;
+            --k;
+        }
+        d.nbr[list_index(s, k + 1, tpa, begin, nr, cap)] = e;
+    }
+}
+
 // Verlet neighbour list with skin: every j (of type >= type i, the
 // reference's t1 <= t2 loop, potential.rs:171-172) within rlist of i.
 // Per-atom builder, used for brute-mode replicas (the whole box is one cell).
 __device__ void phase_build_list(const Dev& d) {
     __shared__ int smi[32];
-    const int N = d.ntot, cap = d.cap, tpa = d.tpa;
+    const int cap = d.cap;
     const float rl = (float)(d.rlist * (1.0 + 1e-5));
     const float rl2 = rl * rl;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
@@ -793,6 +810,7 @@ __device__ void phase_build_list(const Dev& d) {
         const RepDev& R = tile_rep(d, tl.x);
         if (!R.rebuild || R.mode == MODE_CELLS) continue;  // cell-mode replicas: phase_build_list_cells
         const int s = tl.y + threadIdx.x;
+        const int tpa = R.tpa;
         int cnt = 0;
         if ((int)threadIdx.x < tl.z) {
             const float4 xi = __ldcg(d.mir + s);
@@ -819,7 +837,7 @@ __device__ void phase_build_list(const Dev& d) {
                                 const float ex = xj.x - xi.x + sx, ey = xj.y - xi.y + sy,
                                             ez = xj.z - xi.z + sz;
                                 if (ex * ex + ey * ey + ez * ez < rl2) {
-                                    if (cnt < cap) d.nbr[nbr_index(s, cnt, tpa, N)] = (uint32_t)j | (code << IDX_BITS);
+                                    if (cnt < cap) d.nbr[list_index(s, cnt, tpa, R.begin, R.n, cap)] = (uint32_t)j | (code << IDX_BITS);
                                     ++cnt;
                                 }
                             }
@@ -838,27 +856,13 @@ __device__ void phase_build_list(const Dev& d) {
                         else if (e[a] > 0.5f * L[a]) e[a] -= L[a];
                     }
                     if (e[0] * e[0] + e[1] * e[1] + e[2] * e[2] < rl2) {
-                        if (cnt < cap) d.nbr[nbr_index(s, cnt, tpa, N)] = (uint32_t)j | ((uint32_t)CODE_ZERO << IDX_BITS);
+                        if (cnt < cap) d.nbr[list_index(s, cnt, tpa, R.begin, R.n, cap)] = (uint32_t)j | ((uint32_t)CODE_ZERO << IDX_BITS);
                         ++cnt;
                     }
                 }
             }
             const int n = min(cnt, cap);
-            if (d.refmode) {
-                // the reference's accumulation order: ascending (type, index in type)
-                for (int a = 1; a < n; ++a) {
-                    const uint32_t e = d.nbr[nbr_index(s, a, tpa, N)];
-                    const int key = __ldcg(d.rank + (e & IDX_MASK));
-                    int k = a - 1;
-                    while (k >= 0) {
-                        const uint32_t f = d.nbr[nbr_index(s, k, tpa, N)];
-                        if (__ldcg(d.rank + (f & IDX_MASK)) <= key) break;
-                        d.nbr[nbr_index(s, k + 1, tpa, N)] = f;
-                        --k;
-                    }
-                    d.nbr[nbr_index(s, k + 1, tpa, N)] = e;
-                }
-            }
+            if (d.refmode) sort_list_by_rank(d, s, n, tpa, R.begin, R.n);
             d.nn[s] = n;
             if (cnt > cap) {
                 atomicOr(d.err, E_NLIST);
@@ -870,23 +874,6 @@ __device__ void phase_build_list(const Dev& d) {
     }
 }
 
-// In the reference's order (refmode): ascending (type, index in type), i.e. rank.
-__device__ __forceinline__ void sort_list_by_rank(const Dev& d, int s, int n) {
-    const int N = d.ntot, tpa = d.tpa;
-    for (int a = 1; a < n; ++a) {
-        const uint32_t e = d.nbr[nbr_index(s, a, tpa, N)];
-        const int key = __ldcg(d.rank + (e & IDX_MASK));
-        int k = a - 1;
-        while (k >= 0) {
-            const uint32_t f = d.nbr[nbr_index(s, k, tpa, N)];
-            if (__ldcg(d.rank + (f & IDX_MASK)) <= key) break;
-            d.nbr[nbr_index(s, k + 1, tpa, N)] = f;
-            --k;
-        }
-        d.nbr[nbr_index(s, k + 1, tpa, N)] = e;
-    }
-}
-
 // Cell-mode replicas: one warp per cell.  Each lane owns one atom of the cell
 // (a cell of more than 32 atoms takes several passes); the atoms of the 27
 // neighbour cells are staged through shared memory 32 at a time with
@@ -894,7 +881,7 @@ __device__ __forceinline__ void sort_list_by_rank(const Dev& d, int s, int n) {
 // lanes walk the same candidate sequence.
 __device__ void phase_build_list_cells(const Dev& d) {
     __shared__ float4 stage[TILE / 32][32];
-    const int N = d.ntot, cap = d.cap, tpa = d.tpa;
+    const int cap = d.cap;
     const float rl = (float)(d.rlist * (1.0 + 1e-5));
     const float rl2 = rl * rl;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -910,6 +897,7 @@ __device__ void phase_build_list_cells(const Dev& d) {
         if (local >= nc[0] * nc[1] * nc[2]) continue;   // spare cell capacity
         const long long rbeg = __ldcg(&W->begin);
         const int rn = __ldcg(&W->n);
+        const int tpa = __ldcg(&W->tpa);
         const float cs[3] = {dbl_to_flt_rn(__ldcg(&W->cs[0])), dbl_to_flt_rn(__ldcg(&W->cs[1])),
                              dbl_to_flt_rn(__ldcg(&W->cs[2]))};
         int cx, cy, cz;
@@ -918,16 +906,16 @@ __device__ void phase_build_list_cells(const Dev& d) {
         if (ib < rbeg || ib + in > rbeg + rn) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
         int cmax = 0;
         const bool single = d.single_type != 0;
-        const size_t rowstride = (size_t)N * (size_t)tpa;
+        const size_t rowstride = (size_t)rn * (size_t)tpa;
         for (int g = 0; g < in; g += 32) {
             const int s = ib + g + lane;
             const bool own = g + lane < in;
             const float4 xi = own ? __ldcg(d.mir + s) : make_float4(0.f, 0.f, 0.f, 0.f);
             const int ti = own ? type_of(xi) : 0x7FFFFFFF;
             int cnt = 0;
-            // running output position: entry cnt of atom s lives at
-            // rowp[col], rowp = nbr + (cnt / tpa) * N * tpa + s * tpa, col = cnt % tpa
-            uint32_t* rowp = d.nbr + (size_t)s * (size_t)tpa;
+            // running output position (list_index): entry cnt of atom s lives at
+            // rowp[col], rowp = segment + (cnt / tpa) * n * tpa + (s - begin) * tpa, col = cnt % tpa
+            uint32_t* rowp = d.nbr + (size_t)cap * (size_t)rbeg + (size_t)(s - rbeg) * (size_t)tpa;
             int col = 0;
             for (int dz = -1; dz <= 1; ++dz) {
                 int z = cz + dz; z = z < 0 ? z + nc[2] : (z >= nc[2] ? z - nc[2] : z);
@@ -967,7 +955,7 @@ __device__ void phase_build_list_cells(const Dev& d) {
             }
             if (own) {
                 const int n = min(cnt, cap);
-                if (d.refmode) sort_list_by_rank(d, s, n);
+                if (d.refmode) sort_list_by_rank(d, s, n, tpa, rbeg, rn);
                 d.nn[s] = n;
                 if (cnt > cap) {
                     atomicOr(d.err, E_NLIST);
@@ -1192,7 +1180,7 @@ __global__ void k_pairs(Dev d, long long capacity, int* out_i, int* out_j, unsig
     const int ti = type_of(pi);
     const int n = d.nn[s];
     for (int k = 0; k < n; ++k) {
-        const uint32_t e = d.nbr[nbr_index(s, k, d.tpa, N)];
+        const uint32_t e = d.nbr[list_index(s, k, R.tpa, R.begin, R.n, d.cap)];
         const int j = (int)(e & IDX_MASK);
         if (j < 0 || j >= N) { atomicOr(d.err, E_BOUNDS); continue; }
         const double4_32a pj = d.pos[j];

@@ -61,6 +61,8 @@ struct RepDev {
     long long begin;
     int n, cell_base, cell_cap, tile_begin, ntiles, last_type_count;
     int chunk_begin, nchunks;     // reduction chunks of <= CHUNK_TILES tiles
+    int tpa;                      // threads per atom of this replica's size class (list layout)
+    int size_class;
     int type_off[MAX_TYPES + 1];  // reference order: type t owns ranks [begin+off[t], begin+off[t+1])
     // geometry (device-updated)
     double box[3];
@@ -137,8 +139,10 @@ struct Dev {
     int* slot_of_rank;
     int* bsum;         // [grid] scan block sums
     unsigned int* bar; // [4] grid barrier: count, generation, any_rebuild, pad
-    unsigned int* queue;  // persistent force kernel work counter
-    int* tile_order;   // persistent kernel tile order (costliest first)
+    unsigned int* queue;  // persistent force kernel work counters (one per size class)
+    int* tile_order;   // tiles grouped by size class, costliest first inside a class
+    const int* tile_list;  // the tiles one force launch covers (a size class)
+    int ntile_list, list_class;
 };
 
 __device__ __forceinline__ int type_of(double4_32a p) { return (int)__double_as_longlong(p.w); }
@@ -170,8 +174,13 @@ __device__ __forceinline__ double flt_to_dbl(float f) {
     return __longlong_as_double((long long)((((unsigned long long)mag << 29) + (896ull << 52)) | sign));
 }
 
-__host__ __device__ __forceinline__ size_t nbr_index(int s, int k, int tpa, int ntot) {
-    return ((size_t)(k / tpa) * (size_t)ntot + (size_t)s) * (size_t)tpa + (size_t)(k % tpa);
+// Neighbour entry k of atom s.  Replica r owns the list segment starting at
+// cap * begin_r, laid out [k / tpa][atom][k % tpa] with its own threads per
+// atom, so the tpa lanes of one atom read consecutive words and consecutive
+// atoms of a warp read consecutive groups (coalesced for every tpa).
+__host__ __device__ __forceinline__ size_t list_index(int s, int k, int tpa, long long begin, int n, int cap) {
+    return (size_t)cap * (size_t)begin +
+           ((size_t)(k / tpa) * (size_t)n + (size_t)(s - begin)) * (size_t)tpa + (size_t)(k % tpa);
 }
 
 }  // namespace mdgb

@@ -39,6 +39,8 @@ class Stats:
     force_launches: int = 0
     integrate_ms: float = 0.0
     integrate_launches: int = 0
+    class_threads_per_atom: tuple = (0, 0, 0)
+    class_replicas: tuple = (0, 0, 0)
     extra: dict = field(default_factory=dict)
 
 
@@ -253,7 +255,11 @@ class Engine:
     def stats(self) -> Stats:
         s = _lib.CStats()
         self._check(self._L.mdgb_get_stats(self._h, C.byref(s)))
-        return Stats(**{f: getattr(s, f) for f, _ in _lib.CStats._fields_})
+        vals = {}
+        for f, _ in _lib.CStats._fields_:
+            v = getattr(s, f)
+            vals[f] = tuple(v) if f.startswith("class_") else v
+        return Stats(**vals)
 
     def reset_stats(self):
         self._check(self._L.mdgb_reset_stats(self._h))

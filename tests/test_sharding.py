@@ -52,7 +52,7 @@ def test_two_gloo_ranks():
     import torch.multiprocessing as mp
     world = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
