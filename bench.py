@@ -266,10 +266,21 @@ def run_ours(args):
     eng.close()
 
     if args.legs == "mixed":
+        phases = None
+        if args.trace:
+            te = Engine(precision="mixed", skin=SKIN, trace=True, device=local,
+                        threads_per_atom=st.threads_per_atom)
+            te.set_potential(0, 0, 1.0, 1.0)
+            te.upload(types, end["pos"], end["vel"], [1.0], box)
+            te.compute_forces()
+            te.trace_phases()
+            te.step(args.steps, DT)
+            phases = te.trace_phases()
+            te.close()
         if rank == 0:
             print(json.dumps({"legs": "mixed", "value": value, "ms_per_step": t_ms / args.steps,
                               "force_kernel_ms": force_ms_avg, "threads_per_atom": st.threads_per_atom,
-                              "rebuilds": st.rebuilds, "clocks": clocks}), flush=True)
+                              "rebuilds": st.rebuilds, "clocks": clocks, "k_pre_phases_us": phases}), flush=True)
         return
 
     # ---- end to end through the C ABI with host buffers -------------------
@@ -620,6 +631,7 @@ def main():
                     help="FCC unit cells (default 50,50,100 for lj1m, 100,100,200 for lj8m; profiling uses smaller boxes)")
     ap.add_argument("--legs", default="all", choices=["all", "mixed"],
                     help="'mixed' runs only the timed mixed leg (for profiler captures)")
+    ap.add_argument("--trace", action="store_true", help="with --legs mixed: per-phase times of the step kernel")
     ap.add_argument("--workload", default="lj1m", choices=["lj1m", "argon", "lj8m", "ensemble", "drift"],
                     help="lj1m: the headline 1M-atom box (default); the others are the remaining configurations")
     args = ap.parse_args()

@@ -93,6 +93,8 @@ extern "C" {
 #define MDGB_FLAG_PROFILE 2u
 /* Drive the per-step force pass with the persistent work-queue kernel. */
 #define MDGB_FLAG_PERSISTENT 4u
+/* Record per-phase device time of the step kernel (mdgb_trace_phases). */
+#define MDGB_FLAG_TRACE 8u
 
 typedef struct mdgb_engine mdgb_engine;
 
@@ -212,6 +214,13 @@ MDGB_API int mdgb_ensemble_macro(mdgb_engine* e, int type, mdgb_macro* out_per_r
 MDGB_API int mdgb_interacting_pairs(mdgb_engine* e, int64_t capacity, int32_t* out_i, int32_t* out_j,
                                     int64_t* count);
 MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out);
+/* With MDGB_FLAG_TRACE: microseconds spent in each phase of the per-step
+ * kernel since the last call (then reset), in this order: coupling
+ * reductions, kick/drift, rebuild decision, then (rebuild launches only) zero
+ * cells, bin, scan A, scan B, scan C, scatter, in-cell sort, gather, Verlet
+ * list; then the number of step-kernel launches and of rebuild launches.
+ * Writes min(n, 14) values. */
+MDGB_API int mdgb_trace_phases(mdgb_engine* e, double* out, int n);
 MDGB_API int mdgb_reset_stats(mdgb_engine* e);
 MDGB_API int mdgb_synchronize(mdgb_engine* e);
 

@@ -29,6 +29,9 @@ PRECISION_FP32_NAIVE = 2
 FLAG_REFERENCE_ORDER = 1
 FLAG_PROFILE = 2
 FLAG_PERSISTENT = 4
+FLAG_TRACE = 8
+TRACE_PHASES = ["coupling", "drift", "decide", "zero_cells", "bin", "scan_a", "scan_b", "scan_c", "scatter",
+                "sort_cells", "gather", "verlet_list", "launches", "rebuild_launches"]
 THERMOSTAT_BERENDSEN = 0
 THERMOSTAT_NOSE_HOOVER = 1
 
@@ -106,6 +109,7 @@ SIGNATURES = {
                                          C.POINTER(C.c_int64)]),
     "mdgb_get_stats": (C.c_int, [_E, C.POINTER(CStats)]),
     "mdgb_reset_stats": (C.c_int, [_E]),
+    "mdgb_trace_phases": (C.c_int, [_E, _dp, C.c_int]),
     "mdgb_synchronize": (C.c_int, [_E]),
     "mdgb_forces_noalloc": (C.c_int, [C.c_int64, C.c_void_p, _dp, C.c_double, C.c_double, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),

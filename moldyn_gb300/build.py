@@ -30,6 +30,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ff
 UNITS = [
     ("kernels_step.cu", ["-fmad=false"]),
     ("kernels_force.cu", []),
+    ("kernels_list.cu", []),
     ("engine.cu", []),
     ("host_util.cpp", []),
     ("noalloc.cu", []),

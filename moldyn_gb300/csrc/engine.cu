@@ -101,6 +101,8 @@ struct mdgb_engine {
     double* h_pin = nullptr;     // pinned host staging [11][N]
     int* d_in_i = nullptr;       // [2][N] type, rank
     int* h_err = nullptr;        // pinned
+    unsigned long long* trace_buf = nullptr;  // per-phase ns of k_pre (MDGB_FLAG_TRACE)
+    int lb_grid = 1, lb_cap = -1, lb_ncells = -1;  // list-build launch shape for (cap, cells)
     // coupling (host view of the per-replica settings)
     bool thermo_on = false, baro_on = false, thermo_nh = false;
 
@@ -263,8 +265,14 @@ int launch_pre(mdgb_engine* e, const StepParams& sp) {
     lc.attrs = at;
     lc.numAttrs = 1;
     CU(cudaLaunchKernelEx(&lc, k_pre, e->dev, sp));
+    if (e->lb_cap != e->dev.cap || e->lb_ncells != e->dev.ncells) {
+        e->lb_grid = list_build_grid(e->dev, e->num_sms);
+        e->lb_cap = e->dev.cap;
+        e->lb_ncells = e->dev.ncells;
+    }
+    CU(launch_list_build(e->dev, e->lb_grid, e->stream));
     prof_end(e, pe);
-    e->st.kernel_launches++;
+    e->st.kernel_launches += 2;
     return MDGB_OK;
 }
 
@@ -730,6 +738,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         (rc = dalloc(e, &d.tmp_d, 8 * (size_t)N)) || (rc = dalloc(e, &d.tmp_i, 3 * (size_t)N)) ||
         (rc = dalloc(e, &d.slot_of_rank, N)) || (rc = dalloc(e, &d.bsum, 4096)) ||
         (rc = dalloc(e, &d.bar, 4)) || (rc = dalloc(e, &d.queue, mdgb_engine::NCLASS)) ||
+        (rc = dalloc(e, &e->trace_buf, TR_SLOTS)) ||
         (rc = dalloc(e, &d.tile_order, e->ntiles)) ||
         (rc = dalloc(e, &e->snap_pos, N)) || (rc = dalloc(e, &e->snap_d, 8 * (size_t)N)) ||
         (rc = dalloc(e, &e->snap_i, 4 * (size_t)N)) || (rc = dalloc(e, &e->snap_mir0, N)) ||
@@ -788,6 +797,8 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     CU(cudaMemcpyAsync(d.cell_rep, cell_rep.data(), cell_rep.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream));
     CU(cudaMemsetAsync(d.cell_count, 0, e->ncells * sizeof(int), e->stream));
     CU(cudaMemsetAsync(d.max_needed, 0, sizeof(int), e->stream));
+    CU(cudaMemsetAsync(e->trace_buf, 0, TR_SLOTS * sizeof(unsigned long long), e->stream));
+    d.trace = (e->cfg.flags & MDGB_FLAG_TRACE) ? e->trace_buf : nullptr;
     CU(cudaMemsetAsync(d.err, 0, 2 * sizeof(int), e->stream));
     CU(cudaMemsetAsync(d.bar, 0, 4 * sizeof(unsigned int), e->stream));
     {
@@ -1006,6 +1017,7 @@ MDGB_API int mdgb_create(const mdgb_config* cfg, mdgb_engine** out) {
     int bps2 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps2, (const void*)k_macro, TILE, 0);
     e->pre_blocks_per_sm = std::max(1, std::min(bps, bps2));
+    if (list_build_init() != cudaSuccess) { cudaGetLastError(); delete e; return MDGB_ERR_CUDA; }
     lj_finish(e->pot_default);
     *out = e;
     return MDGB_OK;
@@ -1243,6 +1255,20 @@ MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out) {
         e->st.class_replicas[c] = e->class_nrep[c];
     }
     *out = e->st;
+    return MDGB_OK;
+}
+
+MDGB_API int mdgb_trace_phases(mdgb_engine* e, double* out, int n) {
+    if (!e || !out || n < 0) return MDGB_ERR_INVALID_ARGUMENT;
+    if (!e->has_state) return fail(e, MDGB_ERR_NO_STATE, "no state uploaded");
+    if (!(e->cfg.flags & MDGB_FLAG_TRACE)) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "engine created without MDGB_FLAG_TRACE");
+    cudaSetDevice(e->device);
+    unsigned long long h[TR_SLOTS];
+    CU(cudaMemcpyAsync(h, e->trace_buf, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    CU(cudaMemsetAsync(e->trace_buf, 0, sizeof(h), e->stream));
+    const int m = std::min(n, 14);
+    for (int i = 0; i < m; ++i) out[i] = i < 12 ? h[i] * 1e-3 : (double)h[i];
     return MDGB_OK;
 }
 

@@ -1,0 +1,279 @@
+// kernels_list.cu -- Verlet-list build for cell-mode replicas.
+//
+// Launched right after the step kernel; it returns at once unless that kernel
+// flagged a rebuild (its binning, counting sort and gather have then left the
+// atoms sorted by cell with fresh FP32 mirrors).
+//
+// One warp per cell, 32 of the cell's atoms at a time ("own" atoms, staged in
+// shared memory).  The atoms of the 27 neighbour cells, in shift-code order
+// (dz outer, dx inner) and cell order inside a cell, form one candidate
+// stream.  The warp walks it 32 candidates at a time with one candidate per
+// lane (shifted into the own cell's frame, the next chunk's loads in flight)
+// and tests it against every own atom in turn, collecting a 32-bit mask per
+// lane; a bit transpose across the warp turns these into one hit mask per own
+// atom and chunk, stored in shared memory.  Then each
+// lane expands the masks of its own atom into its list, in stream order --
+// the order a per-atom walk over the 27 cells produces.  All lanes append
+// entry t of their atoms in the same pass, so in the [k / tpa][atom][k % tpa]
+// layout the stores of a pass are contiguous.
+//
+// A pair is listed when its FP32 distance is below rlist (1 + 1e-5): a
+// superset of the pairs inside rlist, which the force kernels decide exactly.
+#include <algorithm>
+
+#include "mdgb_internal.cuh"
+
+namespace mdgb {
+
+constexpr int LB_WARPS = 2;           // warps per block
+constexpr int LB_WIN = 1024;          // candidate stream positions held per window
+constexpr int LB_MQ = LB_WIN / 32 + 1;  // mask row stride (odd: conflict-free columns)
+
+// Per-warp shared memory in 32-bit words: candidate window, hit masks
+// [own atom][chunk], own atoms (float4), the 27 cell shifts (float4).
+constexpr int LB_WARP_WORDS = LB_WIN + 32 * LB_MQ + 32 * 4 + 27 * 4 + 4;
+static_assert((LB_WIN + 32 * LB_MQ) % 4 == 0 && LB_WARP_WORDS % 4 == 0, "float4 alignment");
+
+// Bit-matrix transpose over a warp: lane l holds row l (bit c = entry (l, c));
+// afterwards lane c holds column c (bit l = entry (l, c)).  Five butterfly
+// stages; stage j swaps the off-diagonal j x j blocks of every 2j x 2j block.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane) {
+    const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int st = 0; st < 5; ++st) {
+        const int j = 16 >> st;
+        const uint32_t m = masks[st];
+        const uint32_t p = __shfl_xor_sync(0xffffffffu, x, j);
+        x = (lane & j) ? ((x & ~m) | ((p >> j) & m)) : ((x & m) | ((p & m) << j));
+    }
+    return x;
+}
+
+template <bool SINGLE>
+__global__ void __launch_bounds__(LB_WARPS * 32, 10) k_build_list(Dev d) {
+    if (*(volatile const unsigned int*)(d.bar + 2) == 0u) return;   // no rebuild this step
+    extern __shared__ __align__(16) uint32_t lb_smem[];
+    __shared__ int s_last;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t* cand = lb_smem + (size_t)wib * LB_WARP_WORDS;
+    uint32_t* masks = cand + LB_WIN;
+    float4* own_x = reinterpret_cast<float4*>(masks + 32 * LB_MQ);
+    float4* tab = own_x + 32;
+    const int cap = d.cap;
+    const float rl = (float)(d.rlist * (1.0 + 1e-5));
+    const float rl2 = rl * rl;
+    const int gw = blockIdx.x * LB_WARPS + wib, nw = gridDim.x * LB_WARPS;
+    for (int c = gw; c < d.ncells; c += nw) {
+        const int r = d.cell_rep[c];
+        const RepDev* W = d.rep + r;
+        if (!W->rebuild || W->mode != MODE_CELLS) continue;
+        const int nc[3] = {W->nc[0], W->nc[1], W->nc[2]};
+        const int base = W->cell_base;
+        const int local = c - base;
+        if (local >= nc[0] * nc[1] * nc[2]) continue;   // spare cell capacity
+        const long long rbeg = W->begin;
+        const int rn = W->n, tpa = W->tpa;
+        const int ib = d.cell_start[c], in = d.cell_count[c];
+        if (ib < rbeg || ib + in > rbeg + rn) {
+            if (lane == 0) atomicOr(d.err, E_CELLS);
+            continue;
+        }
+        if (in == 0) continue;
+        int ox, oy, oz;
+        decode_cell(local, nc, ox, oy, oz);
+        __syncwarp();
+        // lane k < 27: neighbour cell with shift code k
+        int nb_start = 0, nb_cnt = 0;
+        if (lane < 27) {
+            const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+            int x = ox + dx; x = x < 0 ? x + nc[0] : (x >= nc[0] ? x - nc[0] : x);
+            int y = oy + dy; y = y < 0 ? y + nc[1] : (y >= nc[1] ? y - nc[1] : y);
+            int z = oz + dz; z = z < 0 ? z + nc[2] : (z >= nc[2] ? z - nc[2] : z);
+            const int cj = base + (x * nc[1] + y) * nc[2] + z;
+            nb_start = d.cell_start[cj];
+            nb_cnt = d.cell_count[cj];
+            if (nb_start < rbeg || nb_start + nb_cnt > rbeg + rn) {
+                atomicOr(d.err, E_CELLS);
+                nb_cnt = 0;
+            }
+            tab[lane] = make_float4((float)dx * dbl_to_flt_rn(W->cs[0]), (float)dy * dbl_to_flt_rn(W->cs[1]),
+                                    (float)dz * dbl_to_flt_rn(W->cs[2]), 0.f);
+        }
+        int incl = nb_cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, off);
+            if (lane >= off) incl += v;
+        }
+        const int nb_off = incl - nb_cnt;
+        const int total = __shfl_sync(FULL, incl, 31);
+        const int self_off = __shfl_sync(FULL, nb_off, CODE_ZERO);   // the own cell's segment
+        int cmax = 0;
+        for (int g = 0; g < in; g += 32) {
+            const int cpc = min(32, in - g);
+            const int s = ib + g + lane;
+            const bool own = lane < cpc;
+            __syncwarp();
+            // rows past the cell's atoms (up to a multiple of 4) sit far away: no hits
+            own_x[lane] = own ? d.mir[s] : make_float4(1e18f, 1e18f, 1e18f, __int_as_float(0x7fffffff));
+            const int cpc4 = (cpc + 3) & ~3;
+            const int pself = self_off + g + lane;   // stream position of the atom itself
+            int cnt = 0;
+            // running output position: entry cnt of atom s is rowp[col],
+            // rowp = segment + (cnt / tpa) * n * tpa + (s - begin) * tpa, col = cnt % tpa
+            uint32_t* rowp = d.nbr + (size_t)cap * (size_t)rbeg + (size_t)(s - rbeg) * (size_t)tpa;
+            const size_t rowstride = (size_t)rn * (size_t)tpa;
+            int col = 0;
+            for (int w0 = 0; w0 < total; w0 += LB_WIN) {
+                const int wn = min(LB_WIN, total - w0);
+                const int nq = (wn + 31) >> 5;
+                __syncwarp();
+                for (int k = 0; k < 27; ++k) {
+                    const int ks = __shfl_sync(FULL, nb_start, k);
+                    const int kn = __shfl_sync(FULL, nb_cnt, k);
+                    const int ko = __shfl_sync(FULL, nb_off, k);
+                    const int lo = max(ko, w0), hi = min(ko + kn, w0 + wn);
+                    for (int p = lo + lane; p < hi; p += 32)
+                        cand[p - w0] = (uint32_t)(ks + p - ko) | ((uint32_t)k << IDX_BITS);
+                }
+                __syncwarp();
+                uint32_t e_n = 0u;
+                float4 x_n = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (lane < wn) {
+                    e_n = cand[lane];
+                    x_n = __ldg(d.mir + (e_n & IDX_MASK));
+                }
+                for (int q = 0; q < nq; ++q) {
+                    const bool valid = (q << 5) + lane < wn;
+                    const float4 sh = tab[e_n >> IDX_BITS];
+                    const float jx = x_n.x + sh.x, jy = x_n.y + sh.y, jz = x_n.z + sh.z;
+                    const int tj = type_of(x_n);
+                    if (((q + 1) << 5) + lane < wn) {   // next chunk in flight
+                        e_n = cand[((q + 1) << 5) + lane];
+                        x_n = __ldg(d.mir + (e_n & IDX_MASK));
+                    }
+                    // bit i of `mine`: own atom i and this lane's candidate are within rlist
+                    uint32_t mine = 0u;
+                    for (int i = 0; i < cpc4; i += 4) {
+                        const uint32_t b0 = 1u << i;
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const float4 xi = own_x[i + u];
+                            const float ex = jx - xi.x, ey = jy - xi.y, ez = jz - xi.z;
+                            const float r2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                            // the reference's t1 <= t2 loop (potential.rs:171-172)
+                            if ((r2 < rl2) & (SINGLE || tj >= type_of(xi))) mine |= b0 << u;
+                        }
+                    }
+                    if (!valid) mine = 0u;
+                    // 32x32 bit transpose across the warp: lane i gets bit k set when
+                    // candidate k of the chunk hits own atom i
+                    mine = warp_transpose32(mine, lane);
+                    masks[lane * LB_MQ + q] = mine;
+                }
+                __syncwarp();
+                // expansion: pass t appends entry t of every lane's atom, so the
+                // stores of a pass land side by side
+                uint32_t* myrow = masks + lane * LB_MQ;
+                int tot = 0;
+                if (own) {
+                    const int ps = pself - w0;
+                    if (ps >= 0 && ps < wn) myrow[ps >> 5] &= ~(1u << (ps & 31));
+                    for (int q = 0; q < nq; ++q) tot += __popc(myrow[q]);
+                }
+                int tmax = tot;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) tmax = max(tmax, __shfl_xor_sync(FULL, tmax, off));
+                uint32_t m = own ? myrow[0] : 0u;
+                int q = 0;
+                if (tpa == 1) {
+                    for (int t = 0; t < tmax; ++t) {
+                        if (t < tot) {
+                            while (m == 0u) m = myrow[++q];   // t < tot: a set bit remains
+                            const int k = __ffs(m) - 1;
+                            m &= m - 1u;
+                            if (cnt + t < cap) *rowp = cand[(q << 5) + k];
+                            rowp += rowstride;
+                        }
+                    }
+                } else {
+                    for (int t = 0; t < tmax; ++t) {
+                        if (t < tot) {
+                            while (m == 0u) m = myrow[++q];
+                            const int k = __ffs(m) - 1;
+                            m &= m - 1u;
+                            if (cnt + t < cap) rowp[col] = cand[(q << 5) + k];
+                            if (++col == tpa) { col = 0; rowp += rowstride; }
+                        }
+                    }
+                }
+                cnt += tot;
+            }
+            if (own) {
+                const int nfill = min(cnt, cap);
+                if (d.refmode) sort_list_by_rank(d, s, nfill, tpa, rbeg, rn);
+                d.nn[s] = nfill;
+                if (cnt > cap) {
+                    atomicOr(d.err, E_NLIST);
+                    atomicMax(d.max_needed, cnt);
+                }
+            }
+            cmax = max(cmax, cnt);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_xor_sync(FULL, cmax, off));
+        if (lane == 0 && cmax > 0) atomicMax(&d.rep[r].max_nn, cmax);
+    }
+    // The last block to finish closes the rebuild of every replica.
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(d.bar + 3, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) {
+            RepDev* W = d.rep + r;
+            if (W->rebuild) {
+                W->rebuild = 0;
+                W->nrebuilds += 1;
+            }
+        }
+        if (threadIdx.x == 0) {
+            if (d.trace) atomicAdd(d.trace + TR_LIST, global_ns() - d.trace[TR_STAMP]);
+            d.bar[3] = 0u;
+            atomicExch(d.bar + 2, 0u);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+constexpr int LB_SMEM = LB_WARPS * LB_WARP_WORDS * 4;
+
+cudaError_t list_build_init() {
+    cudaError_t err = cudaFuncSetAttribute(k_build_list<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, LB_SMEM);
+    if (err != cudaSuccess) return err;
+    return cudaFuncSetAttribute(k_build_list<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, LB_SMEM);
+}
+
+// Grid: every resident warp, no more than one per cell.
+int list_build_grid(const Dev& d, int num_sms) {
+    int bps = 0;
+    const void* fn = d.single_type ? (const void*)k_build_list<true> : (const void*)k_build_list<false>;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, LB_WARPS * 32, LB_SMEM) != cudaSuccess) bps = 1;
+    const int want = (d.ncells + LB_WARPS - 1) / LB_WARPS;
+    return std::max(1, std::min(num_sms * std::max(bps, 1), want));
+}
+
+cudaError_t launch_list_build(const Dev& d, int grid, cudaStream_t st) {
+    if (d.single_type)
+        k_build_list<true><<<grid, LB_WARPS * 32, LB_SMEM, st>>>(d);
+    else
+        k_build_list<false><<<grid, LB_WARPS * 32, LB_SMEM, st>>>(d);
+    return cudaGetLastError();
+}
+
+}  // namespace mdgb

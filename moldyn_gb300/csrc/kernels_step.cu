@@ -41,14 +41,24 @@ __device__ __forceinline__ RepDev load_rep(const RepDev* p) {
 }
 
 // One replica record per block, in shared memory (phases work tile by tile
-// and a tile never straddles replicas).
+// and a tile never straddles replicas).  The copy is kept while consecutive
+// tiles of a block belong to the same replica and dropped at every grid
+// barrier (the next phase may see fields the previous one changed).
 __shared__ RepDev g_tile_rep;
+__shared__ int g_tile_rep_id;
+
+__device__ __forceinline__ void tile_rep_reset() {
+    if (threadIdx.x == 0) g_tile_rep_id = -1;
+    __syncthreads();
+}
 
 __device__ __forceinline__ const RepDev& tile_rep(const Dev& d, int r) {
+    if (g_tile_rep_id == r) return g_tile_rep;   // block-uniform
     __syncthreads();  // every thread is done with the previous tile's record
     const long long* src = reinterpret_cast<const long long*>(d.rep + r);
     long long* dst = reinterpret_cast<long long*>(&g_tile_rep);
     for (int i = threadIdx.x; i < (int)(sizeof(RepDev) / 8); i += blockDim.x) dst[i] = __ldcg(src + i);
+    if (threadIdx.x == 0) g_tile_rep_id = r;
     __syncthreads();
     return g_tile_rep;
 }
@@ -81,6 +91,7 @@ __device__ __forceinline__ void grid_barrier(const Dev& d) {
             }
         }
         __threadfence();
+        g_tile_rep_id = -1;
     }
     __syncthreads();
 }
@@ -168,12 +179,6 @@ __device__ __forceinline__ double warp_sum_tiles(const Dev& d, const RepDev& R, 
     return __shfl_sync(0xffffffffu, s, 0);
 }
 
-__device__ __forceinline__ void decode_cell(int l, const int nc[3], int& cx, int& cy, int& cz) {
-    cz = l % nc[2];
-    const int q = l / nc[2];
-    cy = q % nc[1];
-    cx = q / nc[1];
-}
 
 // FP32 mirror: position relative to the centre of the atom's frozen cell,
 // taken to the nearest periodic image (continuous while the atom stays near
@@ -431,19 +436,31 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
     __shared__ float smx[32];
     __shared__ float tc[7];   // box (FP32), half box, scale since the last rebuild
     const int N = d.ntot;
+    int tc_rep = -1;          // replica tc[] and disp belong to (block-uniform)
+    float disp = 0.f;         // largest displacement seen by this thread in replica tc_rep
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
-        const RepDev& R = tile_rep(d, tl.x);
-        if (threadIdx.x == 0) {
-            for (int a = 0; a < 3; ++a) {
-                tc[a] = dbl_to_flt_rn(R.box[a]);
-                tc[3 + a] = 0.5f * tc[a];
+        if (tl.x != tc_rep) {
+            if (tc_rep >= 0) {
+                const float m = block_max(disp, smx);
+                if (threadIdx.x == 0) atomicMax(&d.rep[tc_rep].max_disp_bits, __float_as_uint(m));
+                disp = 0.f;
             }
-            tc[6] = dbl_to_flt_rn(R.box[0] / R.box_build[0]);
         }
-        __syncthreads();
+        const RepDev& R = tile_rep(d, tl.x);
+        if (tl.x != tc_rep) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int a = 0; a < 3; ++a) {
+                    tc[a] = dbl_to_flt_rn(R.box[a]);
+                    tc[3 + a] = 0.5f * tc[a];
+                }
+                tc[6] = dbl_to_flt_rn(R.box[0] / R.box_build[0]);
+            }
+            __syncthreads();
+            tc_rep = tl.x;
+        }
         const int s = tl.y + threadIdx.x;
-        float disp = 0.f;
         if ((int)threadIdx.x < tl.z) {
             double4_32a p = d.pos[s];
             if (sp.do_drift) {
@@ -492,11 +509,13 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
                     if (dd[a] > tc[3 + a]) dd[a] -= tc[a];
                     else if (dd[a] < -tc[3 + a]) dd[a] += tc[a];
                 }
-                disp = sqrtf(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+                disp = fmaxf(disp, sqrtf(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]));
             }
         }
-        disp = block_max(disp, smx);
-        if (threadIdx.x == 0) atomicMax(&d.rep[tl.x].max_disp_bits, __float_as_uint(disp));
+    }
+    if (tc_rep >= 0) {
+        const float m = block_max(disp, smx);
+        if (threadIdx.x == 0) atomicMax(&d.rep[tc_rep].max_disp_bits, __float_as_uint(m));
     }
 }
 
@@ -657,7 +676,9 @@ __device__ void phase_scan_c(const Dev& d, int chunk) {
     }
 }
 
-__device__ void phase_scatter(const Dev& d) {
+// carry_forces: also move frc/epot/evir (a refresh that no force evaluation
+// follows); a step's force pass rewrites them after the rebuild anyway.
+__device__ void phase_scatter(const Dev& d, bool carry_forces) {
     const int N = d.ntot;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
@@ -673,12 +694,12 @@ __device__ void phase_scatter(const Dev& d) {
         if (slot < R.begin || slot >= R.begin + R.n) { atomicOr(d.err, E_CELLS); continue; }
         d.perm[slot] = s;
         d.tmp_pos[s] = d.pos[s];
-        for (int k = 0; k < 3; ++k) {
-            d.tmp_d[(size_t)k * N + s] = d.vel[(size_t)k * N + s];
-            d.tmp_d[(size_t)(3 + k) * N + s] = d.frc[(size_t)k * N + s];
+        for (int k = 0; k < 3; ++k) d.tmp_d[(size_t)k * N + s] = d.vel[(size_t)k * N + s];
+        if (carry_forces) {
+            for (int k = 0; k < 3; ++k) d.tmp_d[(size_t)(3 + k) * N + s] = d.frc[(size_t)k * N + s];
+            d.tmp_d[(size_t)6 * N + s] = d.epot[s];
+            d.tmp_d[(size_t)7 * N + s] = d.evir[s];
         }
-        d.tmp_d[(size_t)6 * N + s] = d.epot[s];
-        d.tmp_d[(size_t)7 * N + s] = d.evir[s];
         d.tmp_i[s] = d.orig[s];
         d.tmp_i[(size_t)N + s] = d.rank[s];
     }
@@ -747,7 +768,7 @@ __device__ void phase_sort_cells(const Dev& d) {
     }
 }
 
-__device__ void phase_gather(const Dev& d) {
+__device__ void phase_gather(const Dev& d, bool carry_forces) {
     const int N = d.ntot;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
@@ -759,12 +780,12 @@ __device__ void phase_gather(const Dev& d) {
         if (i < R.begin || i >= R.begin + R.n) { atomicOr(d.err, E_BOUNDS); continue; }
         const double4_32a p = ldcg4(d.tmp_pos + i);
         d.pos[s] = p;
-        for (int k = 0; k < 3; ++k) {
-            d.vel[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)k * N + i);
-            d.frc[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)(3 + k) * N + i);
+        for (int k = 0; k < 3; ++k) d.vel[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)k * N + i);
+        if (carry_forces) {
+            for (int k = 0; k < 3; ++k) d.frc[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)(3 + k) * N + i);
+            d.epot[s] = __ldcg(d.tmp_d + (size_t)6 * N + i);
+            d.evir[s] = __ldcg(d.tmp_d + (size_t)7 * N + i);
         }
-        d.epot[s] = __ldcg(d.tmp_d + (size_t)6 * N + i);
-        d.evir[s] = __ldcg(d.tmp_d + (size_t)7 * N + i);
         d.orig[s] = __ldcg(d.tmp_i + i);
         const int rk = __ldcg(d.tmp_i + (size_t)N + i);
         d.rank[s] = rk;
@@ -777,23 +798,6 @@ __device__ void phase_gather(const Dev& d) {
         d.mir0[s] = m;
         if (rk >= 0 && rk < N) d.slot_of_rank[rk] = s;
         else atomicOr(d.err, E_BOUNDS);
-    }
-}
-
-// In the reference's order (refmode): ascending (type, index in type), i.e. rank.
-__device__ __forceinline__ void sort_list_by_rank(const Dev& d, int s, int n, int tpa, long long begin, int nr) {
-    const int cap = d.cap;
-    for (int a = 1; a < n; ++a) {
-        const uint32_t e = d.nbr[list_index(s, a, tpa, begin, nr, cap)];
-        const int key = __ldcg(d.rank + (e & IDX_MASK));
-        int k = a - 1;
-        while (k >= 0) {
-            const uint32_t f = d.nbr[list_index(s, k, tpa, begin, nr, cap)];
-            if (__ldcg(d.rank + (f & IDX_MASK)) <= key) break;
-            d.nbr[list_index(s, k + 1, tpa, begin, nr, cap)] = f;
-            --k;
-        }
-        d.nbr[list_index(s, k + 1, tpa, begin, nr, cap)] = e;
     }
 }
 
@@ -874,115 +878,28 @@ __device__ void phase_build_list(const Dev& d) {
     }
 }
 
-// Cell-mode replicas: one warp per cell.  Each lane owns one atom of the cell
-// (a cell of more than 32 atoms takes several passes); the atoms of the 27
-// neighbour cells are staged through shared memory 32 at a time with
-// coalesced loads and tested by every lane from the broadcast copy, so all
-// lanes walk the same candidate sequence.
-__device__ void phase_build_list_cells(const Dev& d) {
-    __shared__ float4 stage[TILE / 32][32];
-    const int cap = d.cap;
-    const float rl = (float)(d.rlist * (1.0 + 1e-5));
-    const float rl2 = rl * rl;
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int c = gw; c < d.ncells; c += nw) {
-        const int r = d.cell_rep[c];
-        const RepDev* W = d.rep + r;
-        if (!__ldcg(&W->rebuild) || __ldcg(&W->mode) != MODE_CELLS) continue;
-        const int nc[3] = {__ldcg(&W->nc[0]), __ldcg(&W->nc[1]), __ldcg(&W->nc[2])};
-        const int base = __ldcg(&W->cell_base);
-        const int local = c - base;
-        if (local >= nc[0] * nc[1] * nc[2]) continue;   // spare cell capacity
-        const long long rbeg = __ldcg(&W->begin);
-        const int rn = __ldcg(&W->n);
-        const int tpa = __ldcg(&W->tpa);
-        const float cs[3] = {dbl_to_flt_rn(__ldcg(&W->cs[0])), dbl_to_flt_rn(__ldcg(&W->cs[1])),
-                             dbl_to_flt_rn(__ldcg(&W->cs[2]))};
-        int cx, cy, cz;
-        decode_cell(local, nc, cx, cy, cz);
-        const int ib = __ldcg(d.cell_start + c), in = __ldcg(d.cell_count + c);
-        if (ib < rbeg || ib + in > rbeg + rn) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
-        int cmax = 0;
-        const bool single = d.single_type != 0;
-        const size_t rowstride = (size_t)rn * (size_t)tpa;
-        for (int g = 0; g < in; g += 32) {
-            const int s = ib + g + lane;
-            const bool own = g + lane < in;
-            const float4 xi = own ? __ldcg(d.mir + s) : make_float4(0.f, 0.f, 0.f, 0.f);
-            const int ti = own ? type_of(xi) : 0x7FFFFFFF;
-            int cnt = 0;
-            // running output position (list_index): entry cnt of atom s lives at
-            // rowp[col], rowp = segment + (cnt / tpa) * n * tpa + (s - begin) * tpa, col = cnt % tpa
-            uint32_t* rowp = d.nbr + (size_t)cap * (size_t)rbeg + (size_t)(s - rbeg) * (size_t)tpa;
-            int col = 0;
-            for (int dz = -1; dz <= 1; ++dz) {
-                int z = cz + dz; z = z < 0 ? z + nc[2] : (z >= nc[2] ? z - nc[2] : z);
-                for (int dy = -1; dy <= 1; ++dy) {
-                    int y = cy + dy; y = y < 0 ? y + nc[1] : (y >= nc[1] ? y - nc[1] : y);
-                    for (int dx = -1; dx <= 1; ++dx) {
-                        int x = cx + dx; x = x < 0 ? x + nc[0] : (x >= nc[0] ? x - nc[0] : x);
-                        const int cj = base + (x * nc[1] + y) * nc[2] + z;
-                        const uint32_t code = (uint32_t)((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
-                        // candidate displacement = xj - (xi - shift)
-                        const float bx = xi.x - (float)dx * cs[0], by = xi.y - (float)dy * cs[1],
-                                    bz = xi.z - (float)dz * cs[2];
-                        const uint32_t tag = code << IDX_BITS;
-                        const int jb = __ldcg(d.cell_start + cj), jn = __ldcg(d.cell_count + cj);
-                        if (jb < rbeg || jb + jn > rbeg + rn) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
-                        for (int kk = 0; kk < jn; kk += 32) {
-                            const int m = min(32, jn - kk);
-                            __syncwarp();
-                            if (lane < m) stage[wib][lane] = __ldcg(d.mir + jb + kk + lane);
-                            __syncwarp();
-#pragma unroll 2
-                            for (int k = 0; k < m; ++k) {
-                                const float4 xj = stage[wib][k];
-                                const int j = jb + kk + k;
-                                const float ex = xj.x - bx, ey = xj.y - by, ez = xj.z - bz;
-                                const bool take = own && j != s && (single || type_of(xj) >= ti) &&
-                                                  ex * ex + ey * ey + ez * ez < rl2;
-                                if (take) {
-                                    if (cnt < cap) rowp[col] = (uint32_t)j | tag;
-                                    ++cnt;
-                                    if (++col == tpa) { col = 0; rowp += rowstride; }
-                                }
-                            }
-                        }
-                    }
-                }
-            }
-            if (own) {
-                const int n = min(cnt, cap);
-                if (d.refmode) sort_list_by_rank(d, s, n, tpa, rbeg, rn);
-                d.nn[s] = n;
-                if (cnt > cap) {
-                    atomicOr(d.err, E_NLIST);
-                    atomicMax(d.max_needed, cnt);
-                }
-            }
-            cmax = max(cmax, cnt);
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) cmax = max(cmax, __shfl_down_sync(0xffffffffu, cmax, off));
-        if (lane == 0 && cmax > 0) atomicMax(&d.rep[r].max_nn, cmax);
-    }
-}
-
-__device__ void phase_rebuild_done(const Dev& d) {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nt = gridDim.x * blockDim.x;
-    for (int r = gt; r < d.nrep; r += nt) {
-        RepDev* W = d.rep + r;
-        if (__ldcg(&W->rebuild)) { W->rebuild = 0; W->nrebuilds += 1; }
-    }
-    if (gt == 0) atomicExch(d.bar + 2, 0u);
-}
-
 // ---------------------------------------------------------------------------
 // The per-step cooperative kernel.  Block = TILE threads.
+// Phase timing for MDGB_FLAG_TRACE: block 0 stamps the time after each grid
+// barrier (all blocks have finished the phase by then).
+struct PhaseClock {
+    unsigned long long* tr;
+    unsigned long long last;
+    __device__ __forceinline__ explicit PhaseClock(unsigned long long* t)
+        : tr((blockIdx.x == 0 && threadIdx.x == 0) ? t : nullptr), last(0) {
+        if (tr) { last = global_ns(); atomicAdd(tr + TR_LAUNCHES, 1ull); }
+    }
+    __device__ __forceinline__ void mark(int slot) {
+        if (!tr) return;
+        const unsigned long long now = global_ns();
+        atomicAdd(tr + slot, now - last);
+        last = now;
+    }
+};
+
 __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
+    tile_rep_reset();
+    PhaseClock clk(d.trace);
     if (sp.do_drift && sp.coupled) {
         const int sel = d.last_type;
         if (d.refmode) {
@@ -1002,6 +919,7 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
             phase_finalize2(d, sp, true, sel);
             grid_barrier(d);
         }
+        clk.mark(TR_COUPLING);
     }
     if (sp.do_drift && sp.thermo_nh) {
         const int sel = d.last_type;
@@ -1029,35 +947,47 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
         phase_drift(d, sp, false);
     }
     grid_barrier(d);
+    clk.mark(TR_DRIFT);
     phase_decide(d, sp);
     grid_barrier(d);
+    clk.mark(TR_DECIDE);
     if (*(volatile unsigned int*)(d.bar + 2) == 0u) return;
+    if (clk.tr) atomicAdd(clk.tr + TR_REBUILD_LAUNCHES, 1ull);
     phase_zero_cells(d);
     grid_barrier(d);
+    clk.mark(TR_ZERO);
     phase_bin(d);
     grid_barrier(d);
+    clk.mark(TR_BIN);
     const int chunk = (d.ncells + gridDim.x - 1) / gridDim.x;
     phase_scan_a(d, chunk);
     grid_barrier(d);
+    clk.mark(TR_SCAN_A);
     phase_scan_b(d);
     grid_barrier(d);
+    clk.mark(TR_SCAN_B);
     phase_scan_c(d, chunk);
     grid_barrier(d);
-    phase_scatter(d);
+    clk.mark(TR_SCAN_C);
+    phase_scatter(d, !sp.do_drift);
     grid_barrier(d);
+    clk.mark(TR_SCATTER);
     phase_sort_cells(d);
     grid_barrier(d);
-    phase_gather(d);
+    clk.mark(TR_SORT);
+    phase_gather(d, !sp.do_drift);
     grid_barrier(d);
+    clk.mark(TR_GATHER);
+    if (clk.tr) clk.tr[TR_STAMP] = clk.last;
+    // brute-mode replicas here; cell-mode replicas in k_build_list, which
+    // follows this kernel and closes the rebuild
     phase_build_list(d);
-    phase_build_list_cells(d);
-    grid_barrier(d);
-    phase_rebuild_done(d);
 }
 
 // Macro parameters of type `sel` (solver/src/macro_parameters): results land
 // in the replica records (vcm, mom, ke, pe, thermal, T, P, count).
 __global__ void __launch_bounds__(TILE) k_macro(Dev d, StepParams sp, int sel) {
+    tile_rep_reset();
     if (d.refmode) {
         phase_serial(d, sp, sel, false);
         return;

@@ -143,7 +143,28 @@ struct Dev {
     int* tile_order;   // tiles grouped by size class, costliest first inside a class
     const int* tile_list;  // the tiles one force launch covers (a size class)
     int ntile_list, list_class;
+    unsigned long long* trace;  // MDGB_FLAG_TRACE: per-phase nanoseconds of k_pre (else null)
 };
+
+// k_pre phases recorded with MDGB_FLAG_TRACE (slot indices)
+enum : int {
+    TR_COUPLING = 0, TR_DRIFT, TR_DECIDE, TR_ZERO, TR_BIN, TR_SCAN_A, TR_SCAN_B, TR_SCAN_C,
+    TR_SCATTER, TR_SORT, TR_GATHER, TR_LIST, TR_LAUNCHES, TR_REBUILD_LAUNCHES,
+    TR_STAMP = 15,   // time stamp the list-build kernel measures from
+    TR_SLOTS = 16
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Verlet-list build for cell-mode replicas (kernels_list.cu): a kernel that
+// follows every k_pre launch and closes the rebuild k_pre started.
+cudaError_t list_build_init();
+int list_build_grid(const Dev& d, int num_sms);
+cudaError_t launch_list_build(const Dev& d, int grid, cudaStream_t st);
 
 __device__ __forceinline__ int type_of(double4_32a p) { return (int)__double_as_longlong(p.w); }
 __device__ __forceinline__ int type_of(float4 p) { return __float_as_int(p.w); }
@@ -181,6 +202,30 @@ __device__ __forceinline__ double flt_to_dbl(float f) {
 __host__ __device__ __forceinline__ size_t list_index(int s, int k, int tpa, long long begin, int n, int cap) {
     return (size_t)cap * (size_t)begin +
            ((size_t)(k / tpa) * (size_t)n + (size_t)(s - begin)) * (size_t)tpa + (size_t)(k % tpa);
+}
+
+__device__ __forceinline__ void decode_cell(int l, const int nc[3], int& cx, int& cy, int& cz) {
+    cz = l % nc[2];
+    const int q = l / nc[2];
+    cy = q % nc[1];
+    cx = q / nc[1];
+}
+
+// In the reference's order (refmode): ascending (type, index in type), i.e. rank.
+__device__ __forceinline__ void sort_list_by_rank(const Dev& d, int s, int n, int tpa, long long begin, int nr) {
+    const int cap = d.cap;
+    for (int a = 1; a < n; ++a) {
+        const uint32_t e = d.nbr[list_index(s, a, tpa, begin, nr, cap)];
+        const int key = __ldcg(d.rank + (e & IDX_MASK));
+        int k = a - 1;
+        while (k >= 0) {
+            const uint32_t f = d.nbr[list_index(s, k, tpa, begin, nr, cap)];
+            if (__ldcg(d.rank + (f & IDX_MASK)) <= key) break;
+            d.nbr[list_index(s, k + 1, tpa, begin, nr, cap)] = f;
+            --k;
+        }
+        d.nbr[list_index(s, k + 1, tpa, begin, nr, cap)] = e;
+    }
 }
 
 }  // namespace mdgb

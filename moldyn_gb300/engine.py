@@ -64,7 +64,7 @@ class Engine:
     def __init__(self, precision: str = "mixed", skin: float = 0.0, rebuild_every: int = 0,
                  threads_per_atom: int = 0, graph_steps: int = 0, neighbor_capacity: int = 0,
                  device: int = 0, reference_order: bool = False, profile: bool = False,
-                 persistent: bool = False):
+                 persistent: bool = False, trace: bool = False):
         L = load()
         cfg = _lib.Config()
         check(L.mdgb_config_default(C.byref(cfg)))
@@ -78,7 +78,8 @@ class Engine:
         cfg.device = int(device)
         cfg.flags = ((_lib.FLAG_REFERENCE_ORDER if reference_order else 0)
                      | (_lib.FLAG_PROFILE if profile else 0)
-                     | (_lib.FLAG_PERSISTENT if persistent else 0))
+                     | (_lib.FLAG_PERSISTENT if persistent else 0)
+                     | (_lib.FLAG_TRACE if trace else 0))
         h = C.c_void_p()
         st = L.mdgb_create(C.byref(cfg), C.byref(h))
         if st != _lib.MDGB_OK:
@@ -260,6 +261,12 @@ class Engine:
             v = getattr(s, f)
             vals[f] = tuple(v) if f.startswith("class_") else v
         return Stats(**vals)
+
+    def trace_phases(self) -> dict:
+        """Per-phase microseconds of the step kernel since the last call (trace=True)."""
+        out = np.zeros(len(_lib.TRACE_PHASES))
+        self._check(self._L.mdgb_trace_phases(self._h, out, len(out)))
+        return dict(zip(_lib.TRACE_PHASES, out.tolist()))
 
     def reset_stats(self):
         self._check(self._L.mdgb_reset_stats(self._h))
