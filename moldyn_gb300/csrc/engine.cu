@@ -103,6 +103,9 @@ struct mdgb_engine {
     int* h_err = nullptr;        // pinned
     unsigned long long* trace_buf = nullptr;  // per-phase ns of k_pre (MDGB_FLAG_TRACE)
     int lb_grid = 1, lb_cap = -1, lb_ncells = -1;  // list-build launch shape for (cap, cells)
+    // the other position / mirror buffer of each pair (fused NVE drift)
+    double4_32a* pos_alt = nullptr;
+    float4* mir_alt = nullptr;
     // coupling (host view of the per-replica settings)
     bool thermo_on = false, baro_on = false, thermo_nh = false;
 
@@ -111,6 +114,7 @@ struct mdgb_engine {
     int graph_len = 0;
     StepParams graph_sp{};
     bool graph_valid = false;
+    int64_t graph_kernels = 0;   // kernel launches one replay of the graph makes
 
     // stats
     mdgb_stats st{};
@@ -284,6 +288,8 @@ int launch_force_class(mdgb_engine* e, const StepParams& sp, bool kick, int c) {
     force_fn fn = force_kernel(tpa, e->cfg.precision, e->dev.single_type != 0, kick, persistent);
     if (!fn) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "threads_per_atom must be 1, 2, 4 or 8");
     Dev d = e->dev;
+    d.pos_next = e->pos_alt;
+    d.mir_next = e->mir_alt;
     d.tile_list = e->dev.tile_order + e->class_tile_off[c];
     d.ntile_list = e->class_ntiles[c];
     d.list_class = c;
@@ -310,6 +316,10 @@ int launch_force(mdgb_engine* e, const StepParams& sp, bool kick) {
         if (rc) return rc;
     }
     prof_end(e, pe);
+    if (kick && sp.fused) {   // the next positions/mirrors are in the other buffers now
+        std::swap(e->dev.pos, e->pos_alt);
+        std::swap(e->dev.mir, e->mir_alt);
+    }
     return MDGB_OK;
 }
 
@@ -435,11 +445,22 @@ int compute_forces_impl(mdgb_engine* e) {
     return fail(e, MDGB_ERR_NEIGHBOR_OVERFLOW, "neighbour list kept overflowing");
 }
 
+// n steps.  NVE chunks fuse each step's first kick and drift into the force
+// pass of the step before (steps 2..nf+1); nf is even, so the position/mirror
+// buffer pair ends the chunk the way round it started (a captured graph stays
+// valid), and the chunk's last step is unfused, leaving the state at a whole
+// step.
 int run_chunk_kernels(mdgb_engine* e, const StepParams& sp, int n) {
+    const bool fusable = sp.do_drift && !sp.coupled && !sp.thermo_nh;
+    const int nf = fusable ? ((n - 1) & ~1) : 0;
     for (int i = 0; i < n; ++i) {
-        int rc = launch_pre(e, sp);
+        StepParams pre = sp;
+        pre.predrifted = (i >= 1 && i <= nf) ? 1 : 0;
+        int rc = launch_pre(e, pre);
         if (rc) return rc;
-        rc = launch_force(e, sp, true);
+        StepParams frc = sp;
+        frc.fused = i < nf ? 1 : 0;
+        rc = launch_force(e, frc, true);
         if (rc) return rc;
     }
     return MDGB_OK;
@@ -456,8 +477,13 @@ int run_chunk(mdgb_engine* e, const StepParams& sp, int n) {
         cudaGraph_t g = nullptr;
         CU(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
         const int64_t launches0 = e->st.kernel_launches;
+        // capture runs nothing: the buffer pair must read as before afterwards
+        double4_32a* const pos0 = e->dev.pos; double4_32a* const pos1 = e->pos_alt;
+        float4* const mir0 = e->dev.mir; float4* const mir1 = e->mir_alt;
         int rc = run_chunk_kernels(e, sp, n);
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+        e->dev.pos = pos0; e->pos_alt = pos1; e->dev.mir = mir0; e->mir_alt = mir1;
+        e->graph_kernels = e->st.kernel_launches - launches0;
         e->st.kernel_launches = launches0;
         if (rc || ce != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -478,7 +504,7 @@ int run_chunk(mdgb_engine* e, const StepParams& sp, int n) {
     }
     CU(cudaGraphLaunch(e->graph, e->stream));
     e->st.graph_launches++;
-    e->st.kernel_launches += 2 * n;
+    e->st.kernel_launches += e->graph_kernels;
     return MDGB_OK;
 }
 
@@ -727,6 +753,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     if ((rc = dalloc(e, &d.pos, N)) || (rc = dalloc(e, &d.vel, 3 * (size_t)N)) ||
         (rc = dalloc(e, &d.frc, 3 * (size_t)N)) || (rc = dalloc(e, &d.epot, N)) ||
         (rc = dalloc(e, &d.evir, N)) || (rc = dalloc(e, &d.mir, N)) || (rc = dalloc(e, &d.mir0, N)) ||
+        (rc = dalloc(e, &e->pos_alt, N)) || (rc = dalloc(e, &e->mir_alt, N)) ||
         (rc = dalloc(e, &d.cell, N)) || (rc = dalloc(e, &d.orig, N)) || (rc = dalloc(e, &d.rank, N)) ||
         (rc = dalloc(e, &d.nn, N)) || (rc = dalloc(e, &d.tiles, e->ntiles)) ||
         (rc = dalloc(e, &d.rep, nrep)) || (rc = dalloc(e, &d.part, 8 * (size_t)e->ntiles)) ||

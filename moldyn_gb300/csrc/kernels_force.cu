@@ -131,10 +131,58 @@ __device__ __forceinline__ int next_tile(const Dev& d, bool persistent, int& ite
     return d.tile_list[q];
 }
 
+// Second half kick v += F dt/2m (integrator.rs:49-55).  With sp.fused (NVE
+// chunks) also the next step's first half kick and drift (integrator.rs:30-46)
+// into the other position/mirror buffers -- the step kernel that follows only
+// decides and rebuilds.  Same operations, in the same order, as the unfused
+// kick and drift.  Returns the displacement since the last rebuild.
+__device__ __forceinline__ float kick_and_drift(const Dev& d, const StepParams& sp, const RepDev* R,
+                                                const float* tcs, int s, int ty, double fx, double fy,
+                                                double fz) {
+    const int N = d.ntot;
+    const bool fm = d.mixed != 0;
+    const double c = sp.kick_c[ty];
+    double vx = madd(d.vel[s], fx, c, fm);
+    double vy = madd(d.vel[N + s], fy, c, fm);
+    double vz = madd(d.vel[2 * N + s], fz, c, fm);
+    float disp = 0.f;
+    if (sp.fused) {
+        vx = madd(vx, fx, c, fm);
+        vy = madd(vy, fy, c, fm);
+        vz = madd(vz, fz, c, fm);
+        const double4_32a p = drift_wrap(d.pos[s], vx, vy, vz, sp.dt, R->box, fm);
+        d.pos_next[s] = p;
+        const int cl = d.cell[s] - R->cell_base;
+        if (cl >= 0 && cl < R->nc[0] * R->nc[1] * R->nc[2]) {
+            const float4 m = mirror_of(p, cl, *R, tcs + 3, fm);
+            d.mir_next[s] = m;
+            disp = mirror_disp(m, d.mir0[s], tcs);
+        } else {
+            atomicOr(d.err, E_CELLS);
+        }
+    }
+    d.vel[s] = vx;
+    d.vel[N + s] = vy;
+    d.vel[2 * N + s] = vz;
+    return disp;
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Largest displacement of the warp into the replica's running maximum.
+__device__ __forceinline__ void note_displacement(const Dev& d, int r, float disp) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) disp = fmaxf(disp, __shfl_xor_sync(0xffffffffu, disp, off));
+    if ((threadIdx.x & 31) == 0 && disp > 0.f) atomicMax(&d.rep[r].max_disp_bits, __float_as_uint(disp));
+}
+
 // ---------------------------------------------------------------------------
 template <int TPA, bool KICK, bool PERSIST>
 __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp) {
     __shared__ float4 tab[27];
+    __shared__ float tcs[8];
     __shared__ int s_tile;
     const int N = d.ntot;
     const int a = threadIdx.x / TPA, lane = threadIdx.x % TPA;
@@ -148,6 +196,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
         const int rn = R->n;
         __syncthreads();
         shift_table(tab, R);
+        if (KICK && sp.fused && threadIdx.x == 0) drift_consts(*R, tcs);
         __syncthreads();
         const double box[3] = {R->box[0], R->box[1], R->box[2]};
         const float Lf[3] = {(float)box[0], (float)box[1], (float)box[2]};
@@ -203,16 +252,13 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
             fx = tpa_sum_d<TPA>(fx); fy = tpa_sum_d<TPA>(fy); fz = tpa_sum_d<TPA>(fz);
             pe = tpa_sum_d<TPA>(pe); vr = tpa_sum_d<TPA>(vr);
         }
+        float disp = 0.f;
         if (act && lane == 0) {
             d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
             d.epot[s] = pe; d.evir[s] = vr;
-            if (KICK) {                                                          // integrator.rs:49-55
-                const double c = sp.kick_c[ty];
-                d.vel[s] = __dadd_rn(d.vel[s], __dmul_rn(fx, c));
-                d.vel[N + s] = __dadd_rn(d.vel[N + s], __dmul_rn(fy, c));
-                d.vel[2 * N + s] = __dadd_rn(d.vel[2 * N + s], __dmul_rn(fz, c));
-            }
+            if (KICK) disp = kick_and_drift(d, sp, R, tcs, s, ty, fx, fy, fz);   // integrator.rs:49-55
         }
+        if (KICK && sp.fused) note_displacement(d, tl.x, disp);
     }
 }
 
@@ -279,8 +325,11 @@ __device__ __forceinline__ bool exact_pair(const Dev& d, const RepDev* R, int s,
 }
 
 template <int TPA, bool SINGLE, bool KICK, bool PERSIST, bool NAIVE = false>
-__global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp) {
+// 9 blocks of 128 threads per SM (56 registers): the kernel is latency-bound
+// on its neighbour gathers, so it keeps as many warps resident as it can.
+__global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_force_mixed(Dev d, StepParams sp) {
     __shared__ float4 tab[27];
+    __shared__ float tcs[8];
     __shared__ int s_tile;
     const int N = d.ntot;
     const int a = threadIdx.x / TPA, lane = threadIdx.x % TPA;
@@ -299,10 +348,22 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
         const int rn = R->n;
         __syncthreads();
         shift_table(tab, R);
+        if (KICK && sp.fused && threadIdx.x == 0) drift_consts(*R, tcs);
         __syncthreads();
         const bool brute = R->mode == MODE_BRUTE;
         const int s = tl.y + a;
         const bool act = a < tl.z;
+        if (KICK && act && lane == 0) {
+            // the epilogue's operands: in L2 by the time the pair loop is done
+            prefetch_l2(d.vel + s);
+            prefetch_l2(d.vel + N + s);
+            prefetch_l2(d.vel + 2 * N + s);
+            if (sp.fused) {
+                prefetch_l2(d.pos + s);
+                prefetch_l2(d.mir0 + s);
+                prefetch_l2(d.cell + s);
+            }
+        }
         MixedAcc<NAIVE> acc;
         acc.init();
         int ty = 0;
@@ -417,19 +478,16 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_mixed(Dev d, StepParams sp
             }
             pe = tpa_sum_f<TPA>(pe); vr = tpa_sum_f<TPA>(vr);
         }
+        float disp = 0.f;
         if (act && lane == 0) {
             const double fx = NAIVE ? flt_to_dbl(nfx) : fixed_to_double(sx, d.fscale_log2);
             const double fy = NAIVE ? flt_to_dbl(nfy) : fixed_to_double(sy, d.fscale_log2);
             const double fz = NAIVE ? flt_to_dbl(nfz) : fixed_to_double(sz, d.fscale_log2);
             d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
             d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr);
-            if (KICK) {
-                const double c = sp.kick_c[ty];
-                d.vel[s] = __dadd_rn(d.vel[s], __dmul_rn(fx, c));
-                d.vel[N + s] = __dadd_rn(d.vel[N + s], __dmul_rn(fy, c));
-                d.vel[2 * N + s] = __dadd_rn(d.vel[2 * N + s], __dmul_rn(fz, c));
-            }
+            if (KICK) disp = kick_and_drift(d, sp, R, tcs, s, ty, fx, fy, fz);
         }
+        if (KICK && sp.fused) note_displacement(d, tl.x, disp);
     }
 }
 

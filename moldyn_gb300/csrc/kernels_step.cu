@@ -180,43 +180,6 @@ __device__ __forceinline__ double warp_sum_tiles(const Dev& d, const RepDev& R, 
 }
 
 
-// FP32 mirror: position relative to the centre of the atom's frozen cell,
-// taken to the nearest periodic image (continuous while the atom stays near
-// its cell; in brute mode the "cell" is the whole box, so it is the wrapped
-// position relative to the box centre).
-__device__ __forceinline__ float4 mirror_of(double4_32a p, int cell_local, const RepDev& R, const float* hL) {
-    int cx, cy, cz;
-    decode_cell(cell_local, R.nc, cx, cy, cz);
-    // cell centre (c + 0.5) * cs; c + 0.5 is exact in FP32 and converts exactly
-    const double c[3] = {flt_to_dbl((float)cx + 0.5f) * R.cs[0], flt_to_dbl((float)cy + 0.5f) * R.cs[1],
-                         flt_to_dbl((float)cz + 0.5f) * R.cs[2]};
-    const double x[3] = {p.x, p.y, p.z};
-    float o[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        double u = x[a] - c[a];
-        float f = dbl_to_flt_rn(u);
-        const float h = hL[a];
-        // nearest image of the atom relative to its cell centre; only atoms that
-        // just crossed the periodic boundary (|u| ~ L) take this branch, far
-        // from the +-L/2 decision edge, so the FP32 comparison decides it
-        if (f >= h) { u -= R.box[a]; f = dbl_to_flt_rn(u); }
-        else if (f < -h) { u += R.box[a]; f = dbl_to_flt_rn(u); }
-        o[a] = f;
-    }
-    return make_float4(o[0], o[1], o[2], __int_as_float(type_of(p)));
-}
-
-// core/src/particle.rs:120-141 with the comparisons done on the bit patterns:
-// for x >= 0 and L > 0 the signed 64-bit order of the bits is the numeric
-// order, and x < 0.0 is "sign bit set and not -0.0".
-__device__ __forceinline__ double wrap_ref(double x, double L) {
-    const long long b = __double_as_longlong(x);
-    if (b < 0 && b != (long long)0x8000000000000000ull) return __dadd_rn(x, L);
-    if (b >= __double_as_longlong(L)) return __dsub_rn(x, L);
-    return x;
-}
-
 // ---------------------------------------------------------------------------
 // Tree-order reductions over atoms of type `sel` (all of one mass m, so m is
 // factored out of the sums and applied once per replica; halving is exact
@@ -428,7 +391,7 @@ __device__ void phase_kick(const Dev& d, const StepParams& sp) {
         const int ty = (int)reinterpret_cast<const long long*>(d.pos + s)[3];
         const double c = sp.kick_c[ty];
         for (int a = 0; a < 3; ++a)
-            d.vel[(size_t)a * N + s] = __dadd_rn(d.vel[(size_t)a * N + s], __dmul_rn(d.frc[(size_t)a * N + s], c));
+            d.vel[(size_t)a * N + s] = madd(d.vel[(size_t)a * N + s], d.frc[(size_t)a * N + s], c, d.mixed != 0);
     }
 }
 
@@ -450,13 +413,7 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
         const RepDev& R = tile_rep(d, tl.x);
         if (tl.x != tc_rep) {
             __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int a = 0; a < 3; ++a) {
-                    tc[a] = dbl_to_flt_rn(R.box[a]);
-                    tc[3 + a] = 0.5f * tc[a];
-                }
-                tc[6] = dbl_to_flt_rn(R.box[0] / R.box_build[0]);
-            }
+            if (threadIdx.x == 0) drift_consts(R, tc);
             __syncthreads();
             tc_rep = tl.x;
         }
@@ -471,9 +428,9 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
                     vx = __ldcg(d.vel + s); vy = __ldcg(d.vel + N + s); vz = __ldcg(d.vel + 2 * N + s);
                 } else {
                     vx = d.vel[s]; vy = d.vel[N + s]; vz = d.vel[2 * N + s];
-                    vx = __dadd_rn(vx, __dmul_rn(d.frc[s], c));         // :30-36 kick
-                    vy = __dadd_rn(vy, __dmul_rn(d.frc[N + s], c));
-                    vz = __dadd_rn(vz, __dmul_rn(d.frc[2 * N + s], c));
+                    vx = madd(vx, d.frc[s], c, d.mixed != 0);           // :30-36 kick
+                    vy = madd(vy, d.frc[N + s], c, d.mixed != 0);
+                    vz = madd(vz, d.frc[2 * N + s], c, d.mixed != 0);
                 }
                 if (R.thermo_on) {                                       // thermostat.rs:54-58
                     vx = __dmul_rn(vx, R.lambda); vy = __dmul_rn(vy, R.lambda);
@@ -485,31 +442,17 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
                     x = __dmul_rn(x, R.pending); y = __dmul_rn(y, R.pending);
                     z = __dmul_rn(z, R.pending);
                 }
-                x = __dadd_rn(x, __dmul_rn(vx, sp.dt));                   // :42-46 drift
-                y = __dadd_rn(y, __dmul_rn(vy, sp.dt));
-                z = __dadd_rn(z, __dmul_rn(vz, sp.dt));
-                // core/src/particle.rs:120-141: a single shift per axis
-                x = wrap_ref(x, R.box[0]);
-                y = wrap_ref(y, R.box[1]);
-                z = wrap_ref(z, R.box[2]);
                 p.x = x; p.y = y; p.z = z;
+                p = drift_wrap(p, vx, vy, vz, sp.dt, R.box, d.mixed != 0);             // :42-46 drift
                 d.pos[s] = p;
             }
             const int cl = d.cell[s] - R.cell_base;
             // cl is out of range only before the first binning (fresh upload);
             // the forced rebuild that follows computes the mirror then.
             if (cl >= 0 && cl < R.nc[0] * R.nc[1] * R.nc[2]) {
-                const float4 m = mirror_of(p, cl, R, tc + 3);
+                const float4 m = mirror_of(p, cl, R, tc + 3, d.mixed != 0);
                 d.mir[s] = m;
-                const float4 m0 = d.mir0[s];
-                const float sc = tc[6];
-                float dd[3] = {m.x - sc * m0.x, m.y - sc * m0.y, m.z - sc * m0.z};
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    if (dd[a] > tc[3 + a]) dd[a] -= tc[a];
-                    else if (dd[a] < -tc[3 + a]) dd[a] += tc[a];
-                }
-                disp = fmaxf(disp, sqrtf(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]));
+                disp = fmaxf(disp, mirror_disp(m, d.mir0[s], tc));
             }
         }
     }
@@ -793,7 +736,7 @@ __device__ void phase_gather(const Dev& d, bool carry_forces) {
         d.cell[s] = cell;
         const float hL[3] = {0.5f * dbl_to_flt_rn(R.box[0]), 0.5f * dbl_to_flt_rn(R.box[1]),
                              0.5f * dbl_to_flt_rn(R.box[2])};
-        const float4 m = mirror_of(p, cell - R.cell_base, R, hL);
+        const float4 m = mirror_of(p, cell - R.cell_base, R, hL, d.mixed != 0);
         d.mir[s] = m;
         d.mir0[s] = m;
         if (rk >= 0 && rk < N) d.slot_of_rank[rk] = s;
@@ -943,7 +886,7 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
             grid_barrier(d);
         }
         phase_drift(d, sp, true);
-    } else {
+    } else if (!sp.predrifted) {
         phase_drift(d, sp, false);
     }
     grid_barrier(d);

@@ -95,6 +95,8 @@ struct StepParams {
     int fixed_interval;        // >0: rebuild every that many steps
     int force_rebuild;         // rebuild every replica now
     int do_drift;              // 0: only (re)build / refresh, no integration
+    int predrifted;            // the previous force pass already kicked and drifted (NVE)
+    int fused;                 // force pass: also the next step's kick and drift (into pos_next/mir_next)
 };
 
 // Everything a kernel needs, passed by value.
@@ -144,6 +146,8 @@ struct Dev {
     const int* tile_list;  // the tiles one force launch covers (a size class)
     int ntile_list, list_class;
     unsigned long long* trace;  // MDGB_FLAG_TRACE: per-phase nanoseconds of k_pre (else null)
+    double4_32a* pos_next;      // fused drift: where the force kernel writes the next positions
+    float4* mir_next;           //   and mirrors (the other buffer of each pair)
 };
 
 // k_pre phases recorded with MDGB_FLAG_TRACE (slot indices)
@@ -209,6 +213,90 @@ __device__ __forceinline__ void decode_cell(int l, const int nc[3], int& cx, int
     const int q = l / nc[2];
     cy = q % nc[1];
     cx = q / nc[1];
+}
+
+// ---------------------------------------------------------------------------
+// Drift arithmetic shared by the step kernel and the force kernel's fused
+// drift; every operation is an explicit round-to-nearest intrinsic, so both
+// translation units (compiled with different contraction settings) produce
+// the same bits.
+
+// core/src/particle.rs:120-141 with the comparisons done on the bit patterns:
+// for x >= 0 and L > 0 the signed 64-bit order of the bits is the numeric
+// order, and x < 0.0 is "sign bit set and not -0.0".
+__device__ __forceinline__ double wrap_ref(double x, double L) {
+    const long long b = __double_as_longlong(x);
+    if (b < 0 && b != (long long)0x8000000000000000ull) return __dadd_rn(x, L);
+    if (b >= __double_as_longlong(L)) return __dsub_rn(x, L);
+    return x;
+}
+
+// a + b * c: the reference's two roundings (FP64 path) or one fused
+// multiply-add (mixed path: half the operations on GB300's narrow FP64 pipe).
+__device__ __forceinline__ double madd(double a, double b, double c, bool fused) {
+    return fused ? __fma_rn(b, c, a) : __dadd_rn(a, __dmul_rn(b, c));
+}
+
+// integrator.rs:42-46 drift x += v dt, then a single periodic shift per axis.
+__device__ __forceinline__ double4_32a drift_wrap(double4_32a p, double vx, double vy, double vz, double dt,
+                                                  const double* box, bool fused) {
+    p.x = wrap_ref(madd(p.x, vx, dt, fused), box[0]);
+    p.y = wrap_ref(madd(p.y, vy, dt, fused), box[1]);
+    p.z = wrap_ref(madd(p.z, vz, dt, fused), box[2]);
+    return p;
+}
+
+// FP32 mirror: position relative to the centre of the atom's frozen cell,
+// taken to the nearest periodic image (continuous while the atom stays near
+// its cell; in brute mode the "cell" is the whole box, so it is the wrapped
+// position relative to the box centre).  hL: half box in FP32.
+__device__ __forceinline__ float4 mirror_of(double4_32a p, int cell_local, const RepDev& R, const float* hL,
+                                            bool fused) {
+    int cx, cy, cz;
+    decode_cell(cell_local, R.nc, cx, cy, cz);
+    // cell centre (c + 0.5) * cs; c + 0.5 is exact in FP32 and converts exactly
+    const double k[3] = {flt_to_dbl(-((float)cx + 0.5f)), flt_to_dbl(-((float)cy + 0.5f)),
+                         flt_to_dbl(-((float)cz + 0.5f))};
+    const double x[3] = {p.x, p.y, p.z};
+    float o[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double u = madd(x[a], k[a], R.cs[a], fused);
+        float f = dbl_to_flt_rn(u);
+        const float h = hL[a];
+        // nearest image of the atom relative to its cell centre; only atoms that
+        // just crossed the periodic boundary (|u| ~ L) take this branch, far
+        // from the +-L/2 decision edge, so the FP32 comparison decides it
+        if (f >= h) { u = __dsub_rn(u, R.box[a]); f = dbl_to_flt_rn(u); }
+        else if (f < -h) { u = __dadd_rn(u, R.box[a]); f = dbl_to_flt_rn(u); }
+        o[a] = f;
+    }
+    return make_float4(o[0], o[1], o[2], __int_as_float(type_of(p)));
+}
+
+// Per-replica constants of the displacement check: box (FP32), half box, and
+// the box scale since the last rebuild.
+__device__ __forceinline__ void drift_consts(const RepDev& R, float* tc) {
+    for (int a = 0; a < 3; ++a) {
+        tc[a] = dbl_to_flt_rn(R.box[a]);
+        tc[3 + a] = __fmul_rn(0.5f, tc[a]);
+    }
+    tc[6] = dbl_to_flt_rn(__ddiv_rn(R.box[0], R.box_build[0]));
+}
+
+// Distance moved since the last rebuild (mirror against the rebuild mirror
+// scaled with the box), nearest image.
+__device__ __forceinline__ float mirror_disp(float4 m, float4 m0, const float* tc) {
+    const float sc = tc[6];
+    float dd[3] = {__fsub_rn(m.x, __fmul_rn(sc, m0.x)), __fsub_rn(m.y, __fmul_rn(sc, m0.y)),
+                   __fsub_rn(m.z, __fmul_rn(sc, m0.z))};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (dd[a] > tc[3 + a]) dd[a] = __fsub_rn(dd[a], tc[a]);
+        else if (dd[a] < -tc[3 + a]) dd[a] = __fadd_rn(dd[a], tc[a]);
+    }
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dd[0], dd[0]), __fmul_rn(dd[1], dd[1])),
+                                __fmul_rn(dd[2], dd[2])));
 }
 
 // In the reference's order (refmode): ascending (type, index in type), i.e. rank.
