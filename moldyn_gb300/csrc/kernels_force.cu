@@ -67,15 +67,6 @@ constexpr int FIX_FOLD = 256;                      // most terms per lane the wo
 struct FixAcc {
     unsigned hi, lo;
     __device__ __forceinline__ void init() { hi = lo = 0u; }
-    __device__ __forceinline__ void add(float v) {
-        const float t = v * 1.1920928955078125e-07f;   // v * 2^-23, exact
-        const float a = t + FIX_MAGIC;                  // bits: M + rint(t)
-        const float h = a - FIX_MAGIC;                  // rint(t), exact
-        const float l = fmaf(h, -8388608.0f, v);        // v - h * 2^23, exact
-        const float b = l + FIX_MAGIC;                  // bits: M + rint(l)
-        hi += __float_as_uint(a);
-        lo += __float_as_uint(b);
-    }
     // n terms added: remove the n magic offsets.  With n <= FIX_FOLD the two
     // 32-bit words cannot overflow (|h| <= 2^21, |l| <= 2^22 per term).
     __device__ __forceinline__ long long total(int n) const {
@@ -85,19 +76,59 @@ struct FixAcc {
     }
 };
 
-// Exact int64 -> double for |x| < 2^51 (one FP64 add instead of the slower
-// conversion instruction), then scaled by 2^-k through the exponent field.
-__device__ __forceinline__ double fixed_to_double(long long x, int k) {
-    if (x == 0) return 0.0;
-    double d;
-    if (x > -(1LL << 51) && x < (1LL << 51)) {
-        const long long MB = 0x4338000000000000LL;             // bits of 1.5 * 2^52
-        d = __longlong_as_double(x + MB) - 6755399441055744.0;   // exact integer value
-    } else {
-        d = __ll2double_rn(x);
-    }
-    // |d| >= 1, so subtracting k from the exponent keeps it a normal number
-    return __longlong_as_double(__double_as_longlong(d) - ((long long)k << 52));
+// Two floats in one 64-bit register pair (lo, hi) for GB300's paired FP32
+// instructions (add/sub/mul/fma .f32x2: two IEEE round-to-nearest operations
+// per instruction).
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2(float lo, float hi) {
+    f2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float f2_lo(f2_t v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float f2_hi(f2_t v) { return __uint_as_float((unsigned)(v >> 32)); }
+__device__ __forceinline__ f2_t add2(f2_t a, f2_t b) {
+    f2_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t sub2(f2_t a, f2_t b) {
+    f2_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t mul2(f2_t a, f2_t b) {
+    f2_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t fma2(f2_t a, f2_t b, f2_t c) {
+    f2_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// One term per accumulator pair, with the term already divided by 2^23
+// (t = v / 2^23; the scaling is exact): a = t + M holds M + rint(t) = M + h,
+// l' = t - h is exact (Sterbenz) and fma(l', 2^23, M) = M + rint(v - h 2^23).
+// The x and y components go through the paired instructions together.
+__device__ __forceinline__ void fix_add_xyz(FixAcc& ax, FixAcc& ay, FixAcc& az, f2_t dxy, float dz, float g) {
+    const f2_t M2 = f2(FIX_MAGIC, FIX_MAGIC);
+    const f2_t K2 = f2(8388608.0f, 8388608.0f);
+    const f2_t t2 = mul2(dxy, f2(g, g));
+    const f2_t a2 = add2(t2, M2);
+    const f2_t l2 = sub2(t2, sub2(a2, M2));
+    const f2_t b2 = fma2(l2, K2, M2);
+    ax.hi += (unsigned)a2;
+    ay.hi += (unsigned)(a2 >> 32);
+    ax.lo += (unsigned)b2;
+    ay.lo += (unsigned)(b2 >> 32);
+    const float tz = dz * g;
+    const float az_ = tz + FIX_MAGIC;
+    const float lz = tz - (az_ - FIX_MAGIC);
+    const float bz = fmaf(lz, 8388608.0f, FIX_MAGIC);
+    az.hi += __float_as_uint(az_);
+    az.lo += __float_as_uint(bz);
 }
 
 template <int TPA>
@@ -296,19 +327,21 @@ struct MixedAcc {
         pe = vr = gmax = 0.f;
         n = 0;
     }
-    __device__ __forceinline__ void add(float dx, float dy, float dz, float r2, float fs, float u, float fscale) {
+    // fscale_t: the fixed-point scale divided by 2^23; gmax tracks |fs| * fscale_t
+    __device__ __forceinline__ void add(f2_t dxy, float dz, float r2, float fs, float u, float fscale_t) {
         pe += u;
         vr = fmaf(fs, r2, vr);
         if (NAIVE) {
-            fx = fmaf(dx, fs, fx); fy = fmaf(dy, fs, fy); fz = fmaf(dz, fs, fz);
+            fx = fmaf(f2_lo(dxy), fs, fx); fy = fmaf(f2_hi(dxy), fs, fy); fz = fmaf(dz, fs, fz);
             return;
         }
-        const float g = fs * fscale;
+        const float g = fs * fscale_t;
         gmax = fmaxf(gmax, fabsf(g));
-        ax.add(dx * g);
-        ay.add(dy * g);
-        az.add(dz * g);
+        fix_add_xyz(ax, ay, az, dxy, dz, g);
         ++n;
+    }
+    __device__ __forceinline__ void add(float dx, float dy, float dz, float r2, float fs, float u, float fscale_t) {
+        add(f2(dx, dy), dz, r2, fs, u, fscale_t);
     }
 };
 
@@ -334,10 +367,12 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
     const int N = d.ntot;
     const int a = threadIdx.x / TPA, lane = threadIdx.x % TPA;
     const float fscale = d.fscale;
-    // each term |dx * g| <= rlist * gmax; the magic-number split is exact up to 2^44
+    const float fscale_t = NAIVE ? 1.0f : fscale * 1.1920928955078125e-07f;   // fscale / 2^23 (exact)
+    // each term |dx * g| <= rlist * gmax; the magic-number split is exact up to
+    // 2^44 fixed-point units, i.e. |t| <= 2^21 after the division by 2^23
     const float rl = (float)(d.rlist * 1.01);
-    const float split_limit = 17592186044416.0f / rl;       // 2^44 / rlist
-    const float range_limit = 36028797018963968.0f / rl;    // 2^55 / rlist
+    const float split_limit = 2097152.0f / rl;       // 2^44 / 2^23 / rlist
+    const float range_limit = 4294967296.0f / rl;    // 2^55 / 2^23 / rlist
     int iter = 0;
     for (;;) {
         const int t = next_tile(d, PERSIST, iter, &s_tile);
@@ -376,30 +411,44 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
             if (!brute) {
                 // hot loop: FP32 and integer work only, two candidates in flight
                 bool band = false;
+                const f2_t xixy = f2(xi.x, xi.y);
                 auto pair = [&](uint32_t e, float4 xj) {
                     const float4 sh = tab[e >> IDX_BITS];
-                    const float dx = xj.x - xi.x + sh.x, dy = xj.y - xi.y + sh.y, dz = xj.z - xi.z + sh.z;
+                    const f2_t dxy = add2(sub2(f2(xj.x, xj.y), xixy), f2(sh.x, sh.y));
+                    const float dz = xj.z - xi.z + sh.z;
                     const PairF P = SINGLE ? P0 : pairf(d.pair[ty * MAX_TYPES + type_of(xj)]);
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 > P.rc2_hi) return;
-                    if (r2 >= P.rc2_lo) { band = true; return; }   // decided in FP64 below
+                    const float dx = f2_lo(dxy), dy = f2_hi(dxy);
+                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    if (r2 >= P.rc2_lo) {                              // rare: at or past r_cut
+                        if (r2 <= P.rc2_hi) band = true;               // decided in FP64 below
+                        return;
+                    }
                     float fs, u;
                     lj_f32(P, r2, fs, u);
-                    acc.add(dx, dy, dz, r2, fs, u, fscale);
+                    acc.add(dxy, dz, r2, fs, u, fscale_t);
                 };
-                int k = lane;
-                for (; k + TPA < n; k += 2 * TPA) {
-                    const uint32_t e0 = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
-                    const uint32_t e1 = __ldcs(d.nbr + list_index(s, k + TPA, TPA, rbeg, rn, d.cap));
-                    const float4 x0 = __ldg(d.mir + (e0 & IDX_MASK));
-                    const float4 x1 = __ldg(d.mir + (e1 & IDX_MASK));
-                    pair(e0, x0);
-                    pair(e1, x1);
+                // this lane's entries k = lane, lane + TPA, ...: two per iteration,
+                // the next iteration's two list words already in flight (the list
+                // streams from HBM; the gathers hit L2)
+                const uint32_t* lbase = d.nbr + list_index(s, lane, TPA, rbeg, rn, d.cap);
+                const size_t lstride = (size_t)rn * TPA;
+                const int m = n > lane ? (n - lane + TPA - 1) / TPA : 0;
+                uint32_t ea = 0u, eb = 0u;
+                if (m > 0) ea = __ldcs(lbase);
+                if (m > 1) eb = __ldcs(lbase + lstride);
+                int i = 0;
+                for (; i + 1 < m; i += 2) {
+                    const float4 xa = __ldg(d.mir + (ea & IDX_MASK));
+                    const float4 xb = __ldg(d.mir + (eb & IDX_MASK));
+                    uint32_t na = 0u, nb = 0u;
+                    if (i + 2 < m) na = __ldcs(lbase + (size_t)(i + 2) * lstride);
+                    if (i + 3 < m) nb = __ldcs(lbase + (size_t)(i + 3) * lstride);
+                    pair(ea, xa);
+                    pair(eb, xb);
+                    ea = na;
+                    eb = nb;
                 }
-                if (k < n) {
-                    const uint32_t e0 = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
-                    pair(e0, __ldg(d.mir + (e0 & IDX_MASK)));
-                }
+                if (i < m) pair(ea, __ldg(d.mir + (ea & IDX_MASK)));
                 if (band) {
                     // pairs within 1e-5 of r_cut^2: the reference's FP64 decision
                     for (int k = lane; k < n; k += TPA) {
@@ -407,16 +456,17 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
                         const int j = (int)(e & IDX_MASK);
                         const float4 xj = __ldg(d.mir + j);
                         const float4 sh = tab[e >> IDX_BITS];
-                        float dx = xj.x - xi.x + sh.x, dy = xj.y - xi.y + sh.y, dz = xj.z - xi.z + sh.z;
+                        const f2_t dxy = add2(sub2(f2(xj.x, xj.y), f2(xi.x, xi.y)), f2(sh.x, sh.y));
+                        float dx = f2_lo(dxy), dy = f2_hi(dxy), dz = xj.z - xi.z + sh.z;
                         const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(xj)];
                         const PairF P = pairf(PD);
-                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                         if (r2 > P.rc2_hi || r2 < P.rc2_lo) continue;
                         if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
-                        const float rr2 = dx * dx + dy * dy + dz * dz;
+                        const float rr2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                         float fs, u;
                         lj_f32(P, rr2, fs, u);
-                        acc.add(dx, dy, dz, rr2, fs, u, fscale);
+                        acc.add(dx, dy, dz, rr2, fs, u, fscale_t);
                     }
                 }
             } else {
@@ -428,10 +478,10 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
                     const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(__ldg(d.mir + j))];
                     float dx, dy, dz;
                     if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                     float fs, u;
                     lj_f32(pairf(PD), r2, fs, u);
-                    acc.add(dx, dy, dz, r2, fs, u, fscale);
+                    acc.add(dx, dy, dz, r2, fs, u, fscale_t);
                 }
             }
         }
@@ -455,11 +505,11 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
                 if (brute) {
                     if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
                 } else {
-                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                     if (r2 > P.rc2_hi) continue;
                     if (r2 >= P.rc2_lo && !exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
                 }
-                const float r2 = dx * dx + dy * dy + dz * dz;
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                 float fs, u;
                 lj_f32(P, r2, fs, u);
                 const float g = fs * fscale;

@@ -199,6 +199,22 @@ __device__ __forceinline__ double flt_to_dbl(float f) {
     return __longlong_as_double((long long)((((unsigned long long)mag << 29) + (896ull << 52)) | sign));
 }
 
+// Exact int64 -> double for |x| < 2^53 with integer operations (the top bit
+// found with a count of leading zeros, the mantissa shifted into place), then
+// scaled by 2^-k through the exponent (k small enough that the result stays a
+// normal number); larger |x| take the rounding conversion instruction.
+__device__ __forceinline__ double fixed_to_double(long long x, int k) {
+    if (x == 0) return 0.0;
+    const unsigned long long sign = x < 0 ? 0x8000000000000000ull : 0ull;
+    const unsigned long long m = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
+    if (m >= (1ull << 53))
+        return __longlong_as_double(__double_as_longlong(__ll2double_rn(x)) - ((long long)k << 52));
+    const int lz = __clzll((long long)m);   // >= 11
+    const unsigned long long mant = (m << (lz - 11)) & 0x000FFFFFFFFFFFFFull;
+    const unsigned long long ex = (unsigned long long)(63 - lz + 1023 - k);
+    return __longlong_as_double((long long)(sign | (ex << 52) | mant));
+}
+
 // Neighbour entry k of atom s.  Replica r owns the list segment starting at
 // cap * begin_r, laid out [k / tpa][atom][k % tpa] with its own threads per
 // atom, so the tpa lanes of one atom read consecutive words and consecutive
