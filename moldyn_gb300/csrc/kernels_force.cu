@@ -76,38 +76,6 @@ struct FixAcc {
     }
 };
 
-// Two floats in one 64-bit register pair (lo, hi) for GB300's paired FP32
-// instructions (add/sub/mul/fma .f32x2: two IEEE round-to-nearest operations
-// per instruction).
-typedef unsigned long long f2_t;
-__device__ __forceinline__ f2_t f2(float lo, float hi) {
-    f2_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ float f2_lo(f2_t v) { return __uint_as_float((unsigned)v); }
-__device__ __forceinline__ float f2_hi(f2_t v) { return __uint_as_float((unsigned)(v >> 32)); }
-__device__ __forceinline__ f2_t add2(f2_t a, f2_t b) {
-    f2_t r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2_t sub2(f2_t a, f2_t b) {
-    f2_t r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2_t mul2(f2_t a, f2_t b) {
-    f2_t r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2_t fma2(f2_t a, f2_t b, f2_t c) {
-    f2_t r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
 // One term per accumulator pair, with the term already divided by 2^23
 // (t = v / 2^23; the scaling is exact): a = t + M holds M + rint(t) = M + h,
 // l' = t - h is exact (Sterbenz) and fma(l', 2^23, M) = M + rint(v - h 2^23).

@@ -30,7 +30,8 @@ constexpr int LB_WIN = 1024;          // candidate stream positions held per win
 constexpr int LB_MQ = LB_WIN / 32 + 1;  // mask row stride (odd: conflict-free columns)
 
 // Per-warp shared memory in 32-bit words: candidate window, hit masks
-// [own atom][chunk], own atoms (float4), the 27 cell shifts (float4).
+// [own atom][chunk], own atoms (paired coordinates and types: 4 words each),
+// the 27 cell shifts (float4).
 constexpr int LB_WARP_WORDS = LB_WIN + 32 * LB_MQ + 32 * 4 + 27 * 4 + 4;
 static_assert((LB_WIN + 32 * LB_MQ) % 4 == 0 && LB_WARP_WORDS % 4 == 0, "float4 alignment");
 
@@ -58,8 +59,12 @@ __global__ void __launch_bounds__(LB_WARPS * 32, 10) k_build_list(Dev d) {
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint32_t* cand = lb_smem + (size_t)wib * LB_WARP_WORDS;
     uint32_t* masks = cand + LB_WIN;
-    float4* own_x = reinterpret_cast<float4*>(masks + 32 * LB_MQ);
-    float4* tab = own_x + 32;
+    // own atoms in pairs for the paired FP32 instructions: (x_2p, x_2p+1, y_2p,
+    // y_2p+1), (z_2p, z_2p+1), and their types
+    float4* own_xy = reinterpret_cast<float4*>(masks + 32 * LB_MQ);
+    float2* own_z = reinterpret_cast<float2*>(own_xy + 16);
+    int* own_t = reinterpret_cast<int*>(own_z + 16);
+    float4* tab = reinterpret_cast<float4*>(own_t + 32);
     const int cap = d.cap;
     const float rl = (float)(d.rlist * (1.0 + 1e-5));
     const float rl2 = rl * rl;
@@ -116,7 +121,14 @@ __global__ void __launch_bounds__(LB_WARPS * 32, 10) k_build_list(Dev d) {
             const bool own = lane < cpc;
             __syncwarp();
             // rows past the cell's atoms (up to a multiple of 4) sit far away: no hits
-            own_x[lane] = own ? d.mir[s] : make_float4(1e18f, 1e18f, 1e18f, __int_as_float(0x7fffffff));
+            {
+                const float4 xo = own ? d.mir[s] : make_float4(1e18f, 1e18f, 1e18f, __int_as_float(0x7fffffff));
+                float* oxy = reinterpret_cast<float*>(own_xy) + ((lane >> 1) << 2) + (lane & 1);
+                oxy[0] = xo.x;
+                oxy[2] = xo.y;
+                reinterpret_cast<float*>(own_z)[lane] = xo.z;
+                own_t[lane] = type_of(xo);
+            }
             const int cpc4 = (cpc + 3) & ~3;
             const int pself = self_off + g + lane;   // stream position of the atom itself
             int cnt = 0;
@@ -148,6 +160,7 @@ __global__ void __launch_bounds__(LB_WARPS * 32, 10) k_build_list(Dev d) {
                     const bool valid = (q << 5) + lane < wn;
                     const float4 sh = tab[e_n >> IDX_BITS];
                     const float jx = x_n.x + sh.x, jy = x_n.y + sh.y, jz = x_n.z + sh.z;
+                    const f2_t jx2 = f2(jx, jx), jy2 = f2(jy, jy), jz2 = f2(jz, jz);
                     const int tj = type_of(x_n);
                     if (((q + 1) << 5) + lane < wn) {   // next chunk in flight
                         e_n = cand[((q + 1) << 5) + lane];
@@ -158,12 +171,16 @@ __global__ void __launch_bounds__(LB_WARPS * 32, 10) k_build_list(Dev d) {
                     for (int i = 0; i < cpc4; i += 4) {
                         const uint32_t b0 = 1u << i;
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const float4 xi = own_x[i + u];
-                            const float ex = jx - xi.x, ey = jy - xi.y, ez = jz - xi.z;
-                            const float r2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                        for (int u = 0; u < 4; u += 2) {
+                            // own atoms i+u and i+u+1 against this lane's candidate
+                            const float4 A = own_xy[(i + u) >> 1];
+                            const float2 Z = own_z[(i + u) >> 1];
+                            const f2_t ex = sub2(jx2, f2(A.x, A.y)), ey = sub2(jy2, f2(A.z, A.w)),
+                                       ez = sub2(jz2, f2(Z.x, Z.y));
+                            const f2_t r2 = fma2(ez, ez, fma2(ey, ey, mul2(ex, ex)));
                             // the reference's t1 <= t2 loop (potential.rs:171-172)
-                            if ((r2 < rl2) & (SINGLE || tj >= type_of(xi))) mine |= b0 << u;
+                            if ((f2_lo(r2) < rl2) & (SINGLE || tj >= own_t[i + u])) mine |= b0 << u;
+                            if ((f2_hi(r2) < rl2) & (SINGLE || tj >= own_t[i + u + 1])) mine |= b0 << (u + 1);
                         }
                     }
                     if (!valid) mine = 0u;

@@ -199,6 +199,38 @@ __device__ __forceinline__ double flt_to_dbl(float f) {
     return __longlong_as_double((long long)((((unsigned long long)mag << 29) + (896ull << 52)) | sign));
 }
 
+// Two floats in one 64-bit register pair (lo, hi) for GB300's paired FP32
+// instructions (add/sub/mul/fma .f32x2: two IEEE round-to-nearest operations
+// per instruction).
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2(float lo, float hi) {
+    f2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float f2_lo(f2_t v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float f2_hi(f2_t v) { return __uint_as_float((unsigned)(v >> 32)); }
+__device__ __forceinline__ f2_t add2(f2_t a, f2_t b) {
+    f2_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t sub2(f2_t a, f2_t b) {
+    f2_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t mul2(f2_t a, f2_t b) {
+    f2_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t fma2(f2_t a, f2_t b, f2_t c) {
+    f2_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 // Exact int64 -> double for |x| < 2^53 with integer operations (the top bit
 // found with a count of leading zeros, the mantissa shifted into place), then
 // scaled by 2^-k through the exponent (k small enough that the result stays a
