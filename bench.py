@@ -592,6 +592,51 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_splat(args):
+    """Headless render of the 1M-atom box at 1920x1080 (the GUI viewer's
+    shading through mdgb_splat): frames/s end to end through the C ABI (host
+    particle buffer in, host image out), and the CPU oracle on a small frame."""
+    from moldyn_gb300 import render as rnd
+    from oracle import splat_ref
+    pos, vel, box = make_system(seed=7)
+    n = len(pos)
+    parts = np.zeros((n, 12), dtype=np.float32)
+    parts[:, 0:3] = pos
+    parts[:, 3] = 1.0
+    parts[:, 4:7] = vel
+    parts[:, 7] = 1.0
+    parts[:, 8] = 1.0
+    parts[:, 9] = 0.5
+    parts[:, 10] = np.arange(n) % 3
+    w, h = 1920, 1080
+    cam = rnd.framing_camera(box, w, h)
+    prm = rnd.splat_params(cam, rnd.MODE_SPEED, speed_range=(0.0, 2.5), box=box)
+    for _ in range(args.warmup):
+        rnd.splat(parts, prm, w, h)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        img = rnd.splat(parts, prm, w, h)
+    dt = (time.perf_counter() - t0) / args.steps
+    # oracle: a 64x36 frame of the first 2000 particles, scaled to the same work
+    sub = parts[:2000]
+    cam_s = rnd.framing_camera(box, 64, 36)
+    t0 = time.perf_counter()
+    splat_ref.render(sub, {"view_pos": cam_s.uniform()[0], "view": cam_s.uniform()[1], "proj": cam_s.uniform()[2],
+                           "mode": 1, "box": box, "grange": (0.0, 2.5), "gradient": rnd.DEFAULT_GRADIENT}, 64, 36)
+    t_cpu = time.perf_counter() - t0
+    cpu_pairs_per_s = 64 * 36 * 2000 / t_cpu
+    line = {"metric": "headless frames/s, 1M LJ atoms at 1920x1080 (GUI shading)", "value": 1.0 / dt,
+            "unit": "frames/s", "higher_is_better": True, "steps": args.steps, "warmup": args.warmup,
+            "dtype": "f32", "data": "synthetic: seeded FCC 1M-atom liquid, radius 0.5 sigma",
+            "config": {"workload": "splat_1m_1080p", "atoms": n, "width": w, "height": h, "mode": "speed gradient",
+                       "box_edges": True, "lit_pixels": int((img[:, :, :3].sum(axis=2) > 0.05).sum())},
+            "e2e": {"value": 1.0 / dt, "unit": "frames/s", "h2d_bytes_per_step": int(parts.nbytes),
+                    "d2h_bytes_per_step": int(w * h * 16)},
+            "cpu_baseline": {"value": cpu_pairs_per_s, "unit": "pixel-particle tests/s", "cores": 1, "kind": "port",
+                             "sample": "oracle/splat_ref.py, 64x36 frame x 2000 particles, every pixel against every particle"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_drift(args):
     """256,000 atoms (FCC 40^3 cells), NVE at dt* 0.005: total-energy drift of
     the FP32-naive, mixed (FP32 + fixed point) and FP64 paths."""
@@ -650,7 +695,7 @@ def main():
                     help="'mixed' runs only the timed mixed leg (for profiler captures)")
     ap.add_argument("--trace", action="store_true", help="with --legs mixed: per-phase times of the step kernel")
     ap.add_argument("--tpa", type=int, default=0, help="threads per atom of the lj1m mixed leg (0: autotune)")
-    ap.add_argument("--workload", default="lj1m", choices=["lj1m", "argon", "lj8m", "ensemble", "drift"],
+    ap.add_argument("--workload", default="lj1m", choices=["lj1m", "argon", "lj8m", "ensemble", "drift", "splat"],
                     help="lj1m: the headline 1M-atom box (default); the others are the remaining configurations")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -663,7 +708,8 @@ def main():
     elif args.workload == "lj1m":
         run_ours(args)
     else:
-        {"argon": run_argon, "lj8m": run_lj8m, "ensemble": run_ensemble, "drift": run_drift}[args.workload](args)
+        {"argon": run_argon, "lj8m": run_lj8m, "ensemble": run_ensemble, "drift": run_drift,
+         "splat": run_splat}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -31,6 +31,9 @@
  *                             25-99, :155-174), host only
  *   mdgb_maxwell_boltzmann    initialize_velocities_maxwell_boltzmann
  *                             (solver/src/initializer/velocity.rs:6-29), host only, seeded
+ *   mdgb_splat                the GUI viewer's particle + bounding-box render pass
+ *                             (gui/src/visualizer/window.rs:940-990, shader.wgsl,
+ *                             bounding_box.wgsl), headless
  *
  * Conventions: every call returns an int status (MDGB_OK == 0); no C++
  * exception crosses the ABI; mdgb_last_error() gives the message of the last
@@ -244,6 +247,32 @@ MDGB_API int mdgb_synchronize(mdgb_engine* e);
 #define MDGB_NOALLOC_MAX_CELLS 32768
 MDGB_API int mdgb_forces_noalloc(int64_t n, const double* d_pos, const double box[3], double sigma, double eps,
                                  double* d_force, double* d_potential, double* d_temp, void* stream);
+
+/* ---- headless particle render ----------------------------------------- */
+/* Replaces the GUI viewer's render pass (gui/src/visualizer/window.rs:940-990
+ * with shader.wgsl:38-130 and bounding_box.wgsl:26-59) without a graphics
+ * stack: spheres ray-cast into an RGBA float image, nearest sphere per pixel
+ * (lower index on equal depth), shaded as the GUI's fragment shader, box
+ * edges alpha-blended.  Camera fields are the GUI's CameraUniform
+ * (window.rs:61-65, built by CameraUniform::from, window.rs:366-377):
+ * column-major view (look_to_rh) and a symmetric perspective projection. */
+typedef struct {
+    float view_pos[4];          /* eye, w = 1 */
+    float view[16];             /* column-major */
+    float proj[16];             /* column-major cgmath::perspective */
+    float gradient_min[4];      /* VisualizationParameter (shader.wgsl:7-13) */
+    float gradient_mid[4];
+    float gradient_max[4];
+    float gradient_min_max[4];  /* speed range: [0] min, [1] max */
+    uint32_t mode;              /* 0: colour by particle id % 6, 1: speed gradient, else black */
+    int32_t draw_box;           /* blend the bounding-box edges */
+    float box[4];               /* bounding box size (x, y, z); the box spans [0, size] */
+} mdgb_splat_params;
+/* particles: n x 12 floats per particle, the GUI's ParticleDataLite
+ * (window.rs:53-57, :340-350): position xyz1, velocity xyz1, (mass, radius, id, 0).
+ * out_rgba: height x width x 4 floats, row 0 at the top. */
+MDGB_API int mdgb_splat(const float* particles, int64_t n, const mdgb_splat_params* params, int width,
+                        int height, float* out_rgba);
 
 /* ---- host-only helpers (no GPU) ------------------------------------- */
 /* out = {sigma, eps, r_cut, u_cut} */

@@ -74,7 +74,15 @@ class CStats(C.Structure):
                 ("class_threads_per_atom", C.c_int * 3), ("class_replicas", C.c_int * 3)]
 
 
+class CSplatParams(C.Structure):
+    _fields_ = [("view_pos", C.c_float * 4), ("view", C.c_float * 16), ("proj", C.c_float * 16),
+                ("gradient_min", C.c_float * 4), ("gradient_mid", C.c_float * 4),
+                ("gradient_max", C.c_float * 4), ("gradient_min_max", C.c_float * 4),
+                ("mode", C.c_uint32), ("draw_box", C.c_int32), ("box", C.c_float * 4)]
+
+
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _u16p = np.ctypeslib.ndpointer(dtype=np.uint16, flags="C_CONTIGUOUS")
 _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _opt_dp = C.POINTER(C.c_double)
@@ -113,6 +121,7 @@ SIGNATURES = {
     "mdgb_synchronize": (C.c_int, [_E]),
     "mdgb_forces_noalloc": (C.c_int, [C.c_int64, C.c_void_p, _dp, C.c_double, C.c_double, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mdgb_splat": (C.c_int, [_fp, C.c_int64, C.POINTER(CSplatParams), C.c_int, C.c_int, _fp]),
     "mdgb_lj_new": (C.c_int, [C.c_double, C.c_double, _dp]),
     "mdgb_lj_eval": (C.c_int, [_dp, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mdgb_lattice": (C.c_int, [C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_double, _dp, _dp]),

@@ -34,6 +34,7 @@ UNITS = [
     ("engine.cu", []),
     ("host_util.cpp", []),
     ("noalloc.cu", []),
+    ("splat.cu", []),
 ]
 
 

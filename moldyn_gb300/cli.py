@@ -85,6 +85,17 @@ def _parser():
     hg = sub.add_parser("generate-velocities-histogram")
     hg.add_argument("-s", "--state-number", type=int, required=True)
     hg.add_argument("--particle-types", type=int, nargs="+", required=True)
+    rd = sub.add_parser("render", help="headless picture of a saved frame (the GUI viewer's shading)")
+    rd.add_argument("-s", "--state-number", type=int, default=0)
+    rd.add_argument("-o", "--out", required=True, help="output image (binary PPM)")
+    rd.add_argument("--width", type=int, default=1920)
+    rd.add_argument("--height", type=int, default=1080)
+    rd.add_argument("--color-by", choices=["type", "speed"], default="type")
+    rd.add_argument("--speed-range", type=float, nargs=2, default=[0.0, 1.0])
+    rd.add_argument("--eye", type=float, nargs=3, default=None, help="camera position (default: frames the box)")
+    rd.add_argument("--forward", type=float, nargs=3, default=[1.0, 0.0, 0.0])
+    rd.add_argument("--fovy", type=float, default=70.0)
+    rd.add_argument("--no-box", action="store_true")
     return ap
 
 
@@ -288,10 +299,27 @@ def cmd_histogram(args):
                 f.write(",".join(mio.fmt_float(c) for c in v) + "\n")
 
 
+def cmd_render(args):
+    """The GUI viewer's picture of one frame (gui/src/visualizer/window.rs:940-990),
+    rendered on the GPU without a window and written as a PPM image."""
+    from . import render as rnd
+    mio.load_particles(args.file)
+    st = mio.load_state(args.file, args.state_number)
+    if args.eye is None:
+        cam = rnd.framing_camera(st.boundary_box, args.width, args.height, args.fovy)
+        cam.update(cam.eye, args.forward, args.width, args.height)
+    else:
+        cam = rnd.Camera(args.eye, args.fovy, args.width, args.height, args.forward)
+    mode = rnd.MODE_TYPE if args.color_by == "type" else rnd.MODE_SPEED
+    img = rnd.render_state(st, cam, args.width, args.height, mode, speed_range=args.speed_range,
+                           draw_box=not args.no_box)
+    rnd.write_ppm(args.out, img)
+
+
 COMMANDS = {"generate-default-potentials": cmd_generate_default_potentials, "set-potential": cmd_set_potential,
             "initialize": cmd_initialize, "solve": cmd_solve, "solve-macro-parameters": cmd_solve_macro,
             "check-impulse": cmd_check_impulse, "particle-count": cmd_particle_count,
-            "generate-velocities-histogram": cmd_histogram}
+            "generate-velocities-histogram": cmd_histogram, "render": cmd_render}
 
 
 def main(argv=None):
