@@ -83,7 +83,7 @@ def framing_camera(box, width: int, height: int, fovy: float = 70.0) -> Camera:
     """A camera on the -x side of the box looking along +x (the viewer's
     initial direction, camera.rs:28-30) far enough back to see all of it."""
     box = np.asarray(box, dtype=np.float64)
-    half = 0.5 * max(box[1], box[2] * width / height if height else box[2])
+    half = 0.5 * max(box[1], box[2] * height / width if width else box[2])   # screen up = y, right = z
     dist = half / np.tan(np.radians(fovy) / 2.0) * 1.1 + 0.5 * box[0]
     centre = 0.5 * box
     return Camera(eye=(centre[0] - dist, centre[1], centre[2]), fovy=fovy, width=width, height=height)
