@@ -280,6 +280,19 @@ int launch_pre(mdgb_engine* e, const StepParams& sp) {
     return MDGB_OK;
 }
 
+// Blocks of size class c's force launch: one per tile, or (persistent) as
+// many as are resident.
+int force_grid(mdgb_engine* e, int c, bool kick) {
+    const int ntl = e->class_ntiles[c];
+    if (!(e->cfg.flags & MDGB_FLAG_PERSISTENT)) return ntl;
+    const int tpa = e->class_tpa[c];
+    force_fn fn = force_kernel(tpa, e->cfg.precision, e->dev.single_type != 0, kick, true);
+    int bps = 0;
+    if (!fn || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)fn, TILE * tpa, 0) != cudaSuccess)
+        bps = 1;
+    return std::min(ntl, std::max(1, bps) * e->num_sms);
+}
+
 // One force launch per non-empty size class, each with that class's threads
 // per atom (the replicas of a class were listed with the same layout).
 int launch_force_class(mdgb_engine* e, const StepParams& sp, bool kick, int c) {
@@ -293,23 +306,19 @@ int launch_force_class(mdgb_engine* e, const StepParams& sp, bool kick, int c) {
     d.tile_list = e->dev.tile_order + e->class_tile_off[c];
     d.ntile_list = e->class_ntiles[c];
     d.list_class = c;
-    int grid = d.ntile_list;
-    if (persistent) {
-        int bps = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)fn, TILE * tpa, 0));
-        grid = std::min(d.ntile_list, std::max(1, bps) * e->num_sms);
-    }
+    const int grid = force_grid(e, c, kick);
     void* args[] = {(void*)&d, (void*)&sp};
     CU(cudaLaunchKernel((const void*)fn, dim3(grid), dim3(TILE * tpa), args, 0, e->stream));
     e->st.kernel_launches++;
     return MDGB_OK;
 }
 
-int launch_force(mdgb_engine* e, const StepParams& sp, bool kick) {
+int launch_force(mdgb_engine* e, const StepParams& sp_in, bool kick) {
     cudaEvent_t pe;
     prof_begin(e, 0, &pe);
     if (e->cfg.flags & MDGB_FLAG_PERSISTENT)
         CU(cudaMemsetAsync(e->dev.queue, 0, mdgb_engine::NCLASS * sizeof(unsigned int), e->stream));
+    const StepParams& sp = sp_in;
     for (int c = 0; c < mdgb_engine::NCLASS; ++c) {
         if (!e->class_ntiles[c]) continue;
         int rc = launch_force_class(e, sp, kick, c);
@@ -715,7 +724,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         double prod = 1.0;
         for (int a = 0; a < 3; ++a) {
             const double L = boxes[3 * r + a];
-            R.box[a] = L; R.box_build[a] = L; R.cs[a] = L; R.nc[a] = 1;
+            R.box[a] = L; R.box_build[a] = L; R.cs[a] = L; R.inv_cs[a] = 1.0 / L; R.nc[a] = 1;
             prod *= std::max(1.0, std::floor(L / (e->rlist * (1.0 + 1e-6))));
         }
         const double vol = boxes[3 * r] * boxes[3 * r + 1] * boxes[3 * r + 2];

@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
     int iter = 0;
     for (;;) {
         const int t = next_tile(d, PERSIST, iter, &s_tile);
-        if (t < 0) return;
+        if (t < 0) break;
         const int4 tl = d.tiles[t];
         const RepDev* R = d.rep + tl.x;
         const long long rbeg = R->begin;
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
     int iter = 0;
     for (;;) {
         const int t = next_tile(d, PERSIST, iter, &s_tile);
-        if (t < 0) return;
+        if (t < 0) break;
         const int4 tl = d.tiles[t];
         const RepDev* R = d.rep + tl.x;
         const long long rbeg = R->begin;

@@ -31,14 +31,6 @@ constexpr double K_B = 1.380648528;  // core/src/lib.rs:15
 
 static_assert(sizeof(RepDev) % 8 == 0, "RepDev must be a whole number of 8-byte words");
 
-__device__ __forceinline__ RepDev load_rep(const RepDev* p) {
-    RepDev r;
-    const long long* src = reinterpret_cast<const long long*>(p);
-    long long* dst = reinterpret_cast<long long*>(&r);
-#pragma unroll 4
-    for (int i = 0; i < (int)(sizeof(RepDev) / 8); ++i) dst[i] = __ldcg(src + i);
-    return r;
-}
 
 // One replica record per block, in shared memory (phases work tile by tile
 // and a tile never straddles replicas).  The copy is kept while consecutive
@@ -466,54 +458,7 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
 __device__ void phase_decide(const Dev& d, const StepParams& sp) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int nt = gridDim.x * blockDim.x;
-    for (int r = gt; r < d.nrep; r += nt) {
-        const RepDev R = load_rep(d.rep + r);
-        RepDev* W = d.rep + r;
-        int steps_since = R.steps_since;
-        if (sp.do_drift) {
-            W->pending = R.baro_on ? R.myu : 1.0;
-            ++steps_since;
-        }
-        const double sc = R.box[0] / R.box_build[0];
-        const double maxd = (double)__uint_as_float(R.max_disp_bits);
-        // A pair outside the list at the rebuild had r0 >= rlist; it is now at
-        // >= sc*rlist - 2*maxd, which must stay above the largest cutoff.
-        const bool need = sp.force_rebuild || R.rebuild ||
-                          (2.0 * maxd > sc * d.rlist - d.rcmax - 1e-5 * d.rlist) ||
-                          (sp.fixed_interval > 0 && steps_since >= sp.fixed_interval);
-        if (need) {
-            long long nc[3];
-            bool brute = R.cell_cap < 27;
-            for (int a = 0; a < 3; ++a) {
-                nc[a] = (long long)floor(R.box[a] / (d.rlist * (1.0 + 1e-6)));
-                if (nc[a] < 3) brute = true;
-            }
-            if (!brute) {
-                while (nc[0] * nc[1] * nc[2] > (long long)R.cell_cap) {
-                    int a = 0;
-                    if (nc[1] > nc[a]) a = 1;
-                    if (nc[2] > nc[a]) a = 2;
-                    --nc[a];
-                }
-                if (nc[0] < 3 || nc[1] < 3 || nc[2] < 3) brute = true;
-            }
-            if (brute) nc[0] = nc[1] = nc[2] = 1;
-            for (int a = 0; a < 3; ++a) {
-                W->nc[a] = (int)nc[a];
-                W->cs[a] = R.box[a] / (double)nc[a];
-                W->box_build[a] = R.box[a];
-            }
-            W->mode = brute ? MODE_BRUTE : MODE_CELLS;
-            W->max_disp_bits = 0u;
-            W->max_nn = 0;
-            steps_since = 0;
-            W->rebuild = 1;
-            atomicAdd(d.bar + 2, 1u);
-        } else {
-            W->rebuild = 0;
-        }
-        W->steps_since = steps_since;
-    }
+    for (int r = gt; r < d.nrep; r += nt) decide_replica(d, sp, r);
 }
 
 // ---------------------------------------------------------------------------
@@ -542,8 +487,8 @@ __device__ void phase_bin(const Dev& d) {
             const double x[3] = {p.x, p.y, p.z};
             int c[3];
             for (int a = 0; a < 3; ++a) {
-                const double inv = (double)R.nc[a] / R.box[a];
-                int ci = (int)floor(x[a] * inv);
+                // wrapped positions are >= 0: truncation is the floor
+                const int ci = __double2int_rz(__dmul_rn(x[a], R.inv_cs[a]));
                 c[a] = min(max(ci, 0), R.nc[a] - 1);
             }
             local = (c[0] * R.nc[1] + c[1]) * R.nc[2] + c[2];
@@ -840,9 +785,22 @@ struct PhaseClock {
     }
 };
 
+__device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp, PhaseClock& clk);
+
 __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
     tile_rep_reset();
     PhaseClock clk(d.trace);
+    if (sp.predrifted) {
+        // the fused force pass of the previous step kicked and drifted (NVE
+        // chunks): decide, then rebuild or return
+        phase_decide(d, sp);
+        grid_barrier(d);
+        clk.mark(TR_DECIDE);
+        if (*(volatile unsigned int*)(d.bar + 2) == 0u) return;
+        if (clk.tr) atomicAdd(clk.tr + TR_REBUILD_LAUNCHES, 1ull);
+        k_pre_rebuild(d, sp, clk);
+        return;
+    }
     if (sp.do_drift && sp.coupled) {
         const int sel = d.last_type;
         if (d.refmode) {
@@ -886,7 +844,7 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
             grid_barrier(d);
         }
         phase_drift(d, sp, true);
-    } else if (!sp.predrifted) {
+    } else {
         phase_drift(d, sp, false);
     }
     grid_barrier(d);
@@ -896,6 +854,11 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
     clk.mark(TR_DECIDE);
     if (*(volatile unsigned int*)(d.bar + 2) == 0u) return;
     if (clk.tr) atomicAdd(clk.tr + TR_REBUILD_LAUNCHES, 1ull);
+    k_pre_rebuild(d, sp, clk);
+}
+
+// The rebuild phases of k_pre (replicas with their rebuild flag set).
+__device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp, PhaseClock& clk) {
     phase_zero_cells(d);
     grid_barrier(d);
     clk.mark(TR_ZERO);

@@ -68,6 +68,7 @@ struct RepDev {
     double box[3];
     double box_build[3];
     double cs[3];
+    double inv_cs[3];             // nc / box at the rebuild (binning)
     int nc[3];
     int mode;
     // coupling
@@ -345,6 +346,71 @@ __device__ __forceinline__ float mirror_disp(float4 m, float4 m0, const float* t
     }
     return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dd[0], dd[0]), __fmul_rn(dd[1], dd[1])),
                                 __fmul_rn(dd[2], dd[2])));
+}
+
+// A replica record read through L2 (other blocks may have written it in
+// this launch).
+__device__ __forceinline__ RepDev load_rep(const RepDev* p) {
+    RepDev r;
+    const long long* src = reinterpret_cast<const long long*>(p);
+    long long* dst = reinterpret_cast<long long*>(&r);
+#pragma unroll 4
+    for (int i = 0; i < (int)(sizeof(RepDev) / 8); ++i) dst[i] = __ldcg(src + i);
+    return r;
+}
+
+// Per replica: consume the pending barostat factor, decide on a rebuild (and
+// the new cell grid).  A pair outside the list at the rebuild had r0 >= rlist;
+// after a box scale sc and displacements <= maxd it is at >= sc*rlist -
+// 2*maxd, which must stay above the largest cutoff.  Explicit FP64
+// intrinsics: the step kernel and the fused force pass decide alike.
+__device__ __forceinline__ void decide_replica(const Dev& d, const StepParams& sp, int r) {
+    const RepDev R = load_rep(d.rep + r);
+    RepDev* W = d.rep + r;
+    int steps_since = R.steps_since;
+    if (sp.do_drift) {
+        W->pending = R.baro_on ? R.myu : 1.0;
+        ++steps_since;
+    }
+    const double sc = __ddiv_rn(R.box[0], R.box_build[0]);
+    const double maxd = (double)__uint_as_float(R.max_disp_bits);
+    const double limit = __dsub_rn(__dsub_rn(__dmul_rn(sc, d.rlist), d.rcmax), __dmul_rn(1e-5, d.rlist));
+    const bool need = sp.force_rebuild || R.rebuild || (__dmul_rn(2.0, maxd) > limit) ||
+                      (sp.fixed_interval > 0 && steps_since >= sp.fixed_interval);
+    if (need) {
+        long long nc[3];
+        bool brute = R.cell_cap < 27;
+        const double cmin = __dmul_rn(d.rlist, 1.0 + 1e-6);
+        for (int a = 0; a < 3; ++a) {
+            nc[a] = (long long)floor(__ddiv_rn(R.box[a], cmin));
+            if (nc[a] < 3) brute = true;
+        }
+        if (!brute) {
+            while (nc[0] * nc[1] * nc[2] > (long long)R.cell_cap) {
+                int a = 0;
+                if (nc[1] > nc[a]) a = 1;
+                if (nc[2] > nc[a]) a = 2;
+                --nc[a];
+            }
+            if (nc[0] < 3 || nc[1] < 3 || nc[2] < 3) brute = true;
+        }
+        if (brute) nc[0] = nc[1] = nc[2] = 1;
+        for (int a = 0; a < 3; ++a) {
+            W->nc[a] = (int)nc[a];
+            W->cs[a] = __ddiv_rn(R.box[a], (double)nc[a]);
+            W->inv_cs[a] = __ddiv_rn((double)nc[a], R.box[a]);
+            W->box_build[a] = R.box[a];
+        }
+        W->mode = brute ? MODE_BRUTE : MODE_CELLS;
+        W->max_disp_bits = 0u;
+        W->max_nn = 0;
+        steps_since = 0;
+        W->rebuild = 1;
+        atomicAdd(d.bar + 2, 1u);
+    } else {
+        W->rebuild = 0;
+    }
+    W->steps_since = steps_since;
 }
 
 // In the reference's order (refmode): ascending (type, index in type), i.e. rank.
