@@ -199,31 +199,44 @@ __global__ void __launch_bounds__(LB_WARPS * 32, 10) k_build_list(Dev d) {
                     if (ps >= 0 && ps < wn) myrow[ps >> 5] &= ~(1u << (ps & 31));
                     for (int q = 0; q < nq; ++q) tot += __popc(myrow[q]);
                 }
-                int tmax = tot;
+                // entries this window writes (the rest of an overflowing list is
+                // only counted)
+                const int lim = max(0, min(tot, cap - cnt));
+                int lmax = lim;
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) tmax = max(tmax, __shfl_xor_sync(FULL, tmax, off));
-                uint32_t m = own ? myrow[0] : 0u;
-                int q = 0;
+                for (int off = 16; off > 0; off >>= 1) lmax = max(lmax, __shfl_xor_sync(FULL, lmax, off));
                 if (tpa == 1) {
-                    for (int t = 0; t < tmax; ++t) {
-                        if (t < tot) {
-                            while (m == 0u) m = myrow[++q];   // t < tot: a set bit remains
-                            const int k = __ffs(m) - 1;
-                            m &= m - 1u;
-                            if (cnt + t < cap) *rowp = cand[(q << 5) + k];
-                            rowp += rowstride;
+                    // masks bit-reversed: the next entry is the highest set bit
+                    // (one find-leading-one), candidate 32 q + 31 - p
+                    uint32_t mr = own ? __brev(myrow[0]) : 0u;
+                    int qb = 31;
+#pragma unroll 2
+                    for (int t = 0; t < lmax; ++t) {
+                        if (t < lim) {
+                            while (mr == 0u) {   // t < lim <= tot: a set bit remains
+                                qb += 32;
+                                mr = __brev(myrow[qb >> 5]);
+                            }
+                            const int p = 31 - __clz(mr);
+                            mr ^= 1u << p;
+                            rowp[(size_t)t * rowstride] = cand[qb - p];
                         }
                     }
+                    rowp += (size_t)tot * rowstride;
                 } else {
-                    for (int t = 0; t < tmax; ++t) {
-                        if (t < tot) {
+                    uint32_t m = own ? myrow[0] : 0u;
+                    int q = 0;
+                    for (int t = 0; t < lmax; ++t) {
+                        if (t < lim) {
                             while (m == 0u) m = myrow[++q];
                             const int k = __ffs(m) - 1;
                             m &= m - 1u;
-                            if (cnt + t < cap) rowp[col] = cand[(q << 5) + k];
+                            rowp[col] = cand[(q << 5) + k];
                             if (++col == tpa) { col = 0; rowp += rowstride; }
                         }
                     }
+                    // entries counted past the capacity are never written: no
+                    // further window writes either (lim is 0 from here on)
                 }
                 cnt += tot;
             }
