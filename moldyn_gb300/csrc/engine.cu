@@ -34,6 +34,8 @@ __global__ void k_scatter_forces(Dev d, const double*, const double*, const doub
 __global__ void k_pairs(Dev d, long long capacity, int* out_i, int* out_j, unsigned long long* count);
 using force_fn = void (*)(Dev, StepParams);
 force_fn force_kernel(int tpa, int precision, bool single, bool kick, bool persistent);
+using band_fn = void (*)(Dev, StepParams, int);
+band_fn band_kernel(int precision);
 }  // namespace mdgb
 
 using namespace mdgb;
@@ -319,10 +321,22 @@ int launch_force(mdgb_engine* e, const StepParams& sp_in, bool kick) {
     if (e->cfg.flags & MDGB_FLAG_PERSISTENT)
         CU(cudaMemsetAsync(e->dev.queue, 0, mdgb_engine::NCLASS * sizeof(unsigned int), e->stream));
     const StepParams& sp = sp_in;
+    band_fn bk = band_kernel(e->cfg.precision);
+    if (bk) CU(cudaMemsetAsync(e->dev.band_count, 0, sizeof(int), e->stream));
     for (int c = 0; c < mdgb_engine::NCLASS; ++c) {
         if (!e->class_ntiles[c]) continue;
         int rc = launch_force_class(e, sp, kick, c);
         if (rc) return rc;
+    }
+    if (bk) {
+        // the atoms the force launches left: same buffers as they used
+        Dev d = e->dev;
+        d.pos_next = e->pos_alt;
+        d.mir_next = e->mir_alt;
+        int kk = kick ? 1 : 0;
+        void* args[] = {(void*)&d, (void*)&sp, (void*)&kk};
+        CU(cudaLaunchKernel((const void*)bk, dim3(4 * e->num_sms), dim3(128), args, 0, e->stream));
+        e->st.kernel_launches++;
     }
     prof_end(e, pe);
     if (kick && sp.fused) {   // the next positions/mirrors are in the other buffers now
@@ -763,6 +777,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         (rc = dalloc(e, &d.frc, 3 * (size_t)N)) || (rc = dalloc(e, &d.epot, N)) ||
         (rc = dalloc(e, &d.evir, N)) || (rc = dalloc(e, &d.mir, N)) || (rc = dalloc(e, &d.mir0, N)) ||
         (rc = dalloc(e, &e->pos_alt, N)) || (rc = dalloc(e, &e->mir_alt, N)) ||
+        (rc = dalloc(e, &d.band_list, N)) || (rc = dalloc(e, &d.band_count, 1)) ||
         (rc = dalloc(e, &d.cell, N)) || (rc = dalloc(e, &d.orig, N)) || (rc = dalloc(e, &d.rank, N)) ||
         (rc = dalloc(e, &d.nn, N)) || (rc = dalloc(e, &d.tiles, e->ntiles)) ||
         (rc = dalloc(e, &d.rep, nrep)) || (rc = dalloc(e, &d.part, 8 * (size_t)e->ntiles)) ||

@@ -370,6 +370,7 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
         MixedAcc<NAIVE> acc;
         acc.init();
         int ty = 0;
+        bool deferred = false;   // an atom with a pair in the band goes to k_force_band whole
         if (act) {
             const float4 xi = d.mir[s];
             ty = type_of(xi);
@@ -387,10 +388,9 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
                     const PairF P = SINGLE ? P0 : pairf(d.pair[ty * MAX_TYPES + type_of(xj)]);
                     const float dx = f2_lo(dxy), dy = f2_hi(dxy);
                     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    if (r2 >= P.rc2_lo) {                              // rare: at or past r_cut
-                        if (r2 <= P.rc2_hi) band = true;               // decided in FP64 below
-                        return;
-                    }
+                    // within 1e-5 of r_cut^2: the atom is finished by k_force_band
+                    band |= (r2 >= P.rc2_lo) & (r2 <= P.rc2_hi);
+                    if (r2 >= P.rc2_lo) return;
                     float fs, u;
                     lj_f32(P, r2, fs, u);
                     acc.add(dxy, dz, r2, fs, u, fscale_t);
@@ -417,26 +417,7 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
                     eb = nb;
                 }
                 if (i < m) pair(ea, __ldg(d.mir + (ea & IDX_MASK)));
-                if (band) {
-                    // pairs within 1e-5 of r_cut^2: the reference's FP64 decision
-                    for (int k = lane; k < n; k += TPA) {
-                        const uint32_t e = __ldcs(d.nbr + list_index(s, k, TPA, rbeg, rn, d.cap));
-                        const int j = (int)(e & IDX_MASK);
-                        const float4 xj = __ldg(d.mir + j);
-                        const float4 sh = tab[e >> IDX_BITS];
-                        const f2_t dxy = add2(sub2(f2(xj.x, xj.y), f2(xi.x, xi.y)), f2(sh.x, sh.y));
-                        float dx = f2_lo(dxy), dy = f2_hi(dxy), dz = xj.z - xi.z + sh.z;
-                        const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(xj)];
-                        const PairF P = pairf(PD);
-                        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                        if (r2 > P.rc2_hi || r2 < P.rc2_lo) continue;
-                        if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
-                        const float rr2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                        float fs, u;
-                        lj_f32(P, rr2, fs, u);
-                        acc.add(dx, dy, dz, rr2, fs, u, fscale_t);
-                    }
-                }
+                deferred = band;
             } else {
                 // brute mode (a box smaller than three list radii): the reference's
                 // FP64 displacement for every pair -- these replicas are tiny
@@ -453,8 +434,16 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
                 }
             }
         }
+        if (TPA > 1) {
+#pragma unroll
+            for (int off = TPA / 2; off > 0; off >>= 1) deferred |= __shfl_xor_sync(0xffffffffu, deferred, off, TPA);
+        }
+        if (deferred && lane == 0) {
+            const int slot = atomicAdd(d.band_count, 1);
+            d.band_list[slot] = make_int2(s, tl.x);
+        }
         long long sx = acc.ax.total(acc.n), sy = acc.ay.total(acc.n), sz = acc.az.total(acc.n);
-        if (!NAIVE && act && (acc.gmax > split_limit || acc.n > FIX_FOLD)) {
+        if (!NAIVE && act && !deferred && (acc.gmax > split_limit || acc.n > FIX_FOLD)) {
             // a term may exceed the exact range of the split, or the lane summed
             // more terms than the 32-bit words hold: redo this lane's terms with
             // exact float -> int64 conversions (very close pairs, huge lists)
@@ -497,7 +486,7 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
             pe = tpa_sum_f<TPA>(pe); vr = tpa_sum_f<TPA>(vr);
         }
         float disp = 0.f;
-        if (act && lane == 0) {
+        if (act && lane == 0 && !deferred) {
             const double fx = NAIVE ? flt_to_dbl(nfx) : fixed_to_double(sx, d.fscale_log2);
             const double fy = NAIVE ? flt_to_dbl(nfy) : fixed_to_double(sy, d.fscale_log2);
             const double fz = NAIVE ? flt_to_dbl(nfz) : fixed_to_double(sz, d.fscale_log2);
@@ -506,6 +495,99 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
             if (KICK) disp = kick_and_drift(d, sp, R, tcs, s, ty, fx, fy, fz);
         }
         if (KICK && sp.fused) note_displacement(d, tl.x, disp);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Atoms with a pair whose FP32 r^2 lies within 1e-5 of r_cut^2 (about one in
+// six hundred per step): k_force_mixed leaves them (and their kick/drift) to
+// this kernel, so its hot loop carries no FP64 code and no second pass
+// (measured: ~20 % of the force kernel's time).  One warp per atom, lanes
+// over the list; the band pairs are decided with the reference's FP64
+// arithmetic; every term is rounded to fixed point exactly as in
+// k_force_mixed (rint(dx * g), here by the conversion instruction), so the
+// force sums are the ones the main kernel would have produced.  Potential and
+// temp are FP32 sums in a fixed shuffle order.
+template <bool NAIVE>
+__global__ void __launch_bounds__(128) k_force_band(Dev d, StepParams sp, int kick) {
+    const int N = d.ntot;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int count = *(volatile const int*)d.band_count;
+    const float fscale = d.fscale;
+    const float rl = (float)(d.rlist * 1.01);
+    const float range_limit = 36028797018963968.0f / rl;   // 2^55 / rlist
+    for (int w = gw; w < count; w += nw) {
+        const int2 sr = d.band_list[w];
+        const int s = sr.x;
+        const RepDev* R = d.rep + sr.y;
+        const long long rbeg = R->begin;
+        const int rn = R->n, tpa = R->tpa;
+        const float csf[3] = {(float)R->cs[0], (float)R->cs[1], (float)R->cs[2]};
+        const float4 xi = d.mir[s];
+        const int ty = type_of(xi);
+        const int n = d.nn[s];
+        long long sx = 0, sy = 0, sz = 0;
+        float fx = 0.f, fy = 0.f, fz = 0.f, pe = 0.f, vr = 0.f;
+        bool over = false;
+        for (int k = lane; k < n; k += 32) {
+            const uint32_t e = __ldcs(d.nbr + list_index(s, k, tpa, rbeg, rn, d.cap));
+            const int j = (int)(e & IDX_MASK);
+            const float4 xj = __ldg(d.mir + j);
+            const int c = (int)(e >> IDX_BITS);
+            // the shift table of the main kernel (shift_table)
+            const float shx = (float)(c % 3 - 1) * csf[0], shy = (float)((c / 3) % 3 - 1) * csf[1],
+                        shz = (float)(c / 9 - 1) * csf[2];
+            const f2_t dxy = add2(sub2(f2(xj.x, xj.y), f2(xi.x, xi.y)), f2(shx, shy));
+            float dx = f2_lo(dxy), dy = f2_hi(dxy), dz = xj.z - xi.z + shz;
+            const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(xj)];
+            const PairF P = pairf(PD);
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            if (r2 > P.rc2_hi) continue;
+            float rr2 = r2;
+            if (r2 >= P.rc2_lo) {
+                if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
+                rr2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            }
+            float fs, u;
+            lj_f32(P, rr2, fs, u);
+            pe += u;
+            vr = fmaf(fs, rr2, vr);
+            if (NAIVE) {
+                fx = fmaf(dx, fs, fx); fy = fmaf(dy, fs, fy); fz = fmaf(dz, fs, fz);
+            } else {
+                const float g = fs * fscale;
+                over |= fabsf(g) > range_limit;
+                sx += __float2ll_rn(dx * g);
+                sy += __float2ll_rn(dy * g);
+                sz += __float2ll_rn(dz * g);
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            sx += __shfl_down_sync(0xffffffffu, sx, off);
+            sy += __shfl_down_sync(0xffffffffu, sy, off);
+            sz += __shfl_down_sync(0xffffffffu, sz, off);
+            fx += __shfl_down_sync(0xffffffffu, fx, off);
+            fy += __shfl_down_sync(0xffffffffu, fy, off);
+            fz += __shfl_down_sync(0xffffffffu, fz, off);
+            pe += __shfl_down_sync(0xffffffffu, pe, off);
+            vr += __shfl_down_sync(0xffffffffu, vr, off);
+        }
+        if (over) atomicOr(d.err, E_FIXED);
+        if (lane == 0) {
+            const double Fx = NAIVE ? flt_to_dbl(fx) : fixed_to_double(sx, d.fscale_log2);
+            const double Fy = NAIVE ? flt_to_dbl(fy) : fixed_to_double(sy, d.fscale_log2);
+            const double Fz = NAIVE ? flt_to_dbl(fz) : fixed_to_double(sz, d.fscale_log2);
+            d.frc[s] = Fx; d.frc[N + s] = Fy; d.frc[2 * N + s] = Fz;
+            d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr);
+            if (kick) {
+                float tcs[8];
+                drift_consts(*R, tcs);
+                const float disp = kick_and_drift(d, sp, R, tcs, s, ty, Fx, Fy, Fz);
+                if (sp.fused && disp > 0.f) atomicMax(&d.rep[sr.y].max_disp_bits, __float_as_uint(disp));
+            }
+        }
     }
 }
 
@@ -540,6 +622,12 @@ static force_fn pick_persist(int tpa, int precision, bool single, bool kick) {
         case 8: return pick_tpa<8, PERSIST>(precision, single, kick);
         default: return nullptr;
     }
+}
+
+using band_fn = void (*)(Dev, StepParams, int);
+band_fn band_kernel(int precision) {
+    if (precision == 0) return nullptr;
+    return precision == 2 ? (band_fn)k_force_band<true> : (band_fn)k_force_band<false>;
 }
 
 force_fn force_kernel(int tpa, int precision, bool single, bool kick, bool persistent) {

@@ -149,6 +149,8 @@ struct Dev {
     unsigned long long* trace;  // MDGB_FLAG_TRACE: per-phase nanoseconds of k_pre (else null)
     double4_32a* pos_next;      // fused drift: where the force kernel writes the next positions
     float4* mir_next;           //   and mirrors (the other buffer of each pair)
+    int2* band_list;            // mixed path: atoms (index, replica) left to k_force_band
+    int* band_count;
 };
 
 // k_pre phases recorded with MDGB_FLAG_TRACE (slot indices)
