@@ -210,6 +210,52 @@ def test_mixed_forces_error(mdgb, oracle, name, tpa):
     e.close()
 
 
+def _cutoff_pairs():
+    """Isolated pairs whose separations straddle r_cut = 2.5 sigma by a few
+    parts in 1e7..1e6 (inside the mixed path's 1e-5 band, where FP32 cannot
+    decide), along an axis and along a diagonal, 7 sigma apart."""
+    deltas = [-3e-6, -1e-6, -2e-7, 0.0, 2e-7, 1e-6, 3e-6]
+    dirs = [np.array([1.0, 0.0, 0.0]), np.array([1.0, 1.0, 1.0]) / np.sqrt(3.0)]
+    pos = []
+    k = 0
+    for dv in dirs:
+        for dl in deltas:
+            g = np.array([k % 4, (k // 4) % 4, k // 16], dtype=np.float64) * 7.0 + 1.0
+            pos.append(g)
+            pos.append(g + dv * 2.5 * (1.0 + dl))
+            k += 1
+    pos = np.array(pos)
+    box = np.array([28.0, 28.0, 28.0])
+    vel = np.zeros_like(pos)
+    return pos, vel, box
+
+
+@pytest.mark.parametrize("tpa", [1, 2, 8])
+def test_mixed_pairs_at_the_cutoff(mdgb, oracle, tpa):
+    """Pairs within 1e-5 of r_cut^2 are decided with the reference's FP64
+    arithmetic (k_force_band): the mixed path includes exactly the pairs the
+    oracle includes, with forces to the mixed bar, also through fused steps."""
+    pos, vel, box = _cutoff_pairs()
+    ost = _oracle_state(oracle, pos, vel, box)
+    ost.update_force()
+    e = _engine(mdgb, "mixed", threads_per_atom=tpa)
+    _upload(e, pos, vel, box)
+    e.compute_forces()
+    out = e.download()
+    on = np.linalg.norm(ost.force, axis=1) > 0
+    gn = np.linalg.norm(out["force"], axis=1) > 0
+    assert on.any() and (~on).any()          # both sides of the cutoff are present
+    assert np.array_equal(on, gn)
+    assert np.allclose(out["force"], ost.force, rtol=1e-5, atol=1e-7 * np.abs(ost.force).max())
+    # fused NVE steps carry the band atoms' kick and drift too
+    e.step(30, 0.005)
+    ost.step(0.005, nsteps=30)
+    got = e.download()
+    assert np.allclose(got["pos"], ost.pos, rtol=0, atol=1e-9)
+    assert np.allclose(got["vel"], ost.vel, rtol=0, atol=1e-8)
+    e.close()
+
+
 def test_multitype_reference_semantics(mdgb, oracle):
     """Two types with their own LJ pairs; atoms of type t see only types >= t
     (potential.rs:171-176), bit-identical in reference order."""
