@@ -492,7 +492,7 @@ def run_lj8m(args):
     pos, vel, box = make_system(seed=88)
     n = len(pos)
     T0 = T_STAR * 100.0 / K_B
-    e = Engine(precision="mixed", skin=SKIN, profile=True)
+    e = Engine(precision="mixed", skin=SKIN, profile=not args.trace, trace=args.trace)
     e.set_potential(0, 0, 1.0, 1.0)
     e.upload(np.zeros(n, dtype=np.uint16), pos, vel, [1.0], box)
     e.compute_forces()
@@ -500,9 +500,12 @@ def run_lj8m(args):
     kw = dict(thermostat=th, target_temperature=T0, barostat=ba, target_pressure=1.0)
     e.step(args.warmup, DT, **kw)
     e.reset_stats()
+    if args.trace:
+        e.trace_phases()
     with ClockSampler(0) as clk:
         ms = _timed_steps(e, args.steps, DT, **kw)
     st = e.stats()
+    phases = e.trace_phases() if args.trace else None
     mac = e.macro(0)
     end = e.download()
     e.close()
@@ -522,10 +525,14 @@ def run_lj8m(args):
                        "final_P_star": mac["pressure"], "final_box": end["box"].tolist()},
             "clocks": clk.summary(),
             "kernels": {"k_force_mixed": {"avg_ms": f_ms, "bytes_per_atom": BYTES_PER_ATOM_FORCE,
-                                          "achieved_GBps": BYTES_PER_ATOM_FORCE * n / (f_ms * 1e-3) / 1e9,
+                                          "achieved_GBps": (BYTES_PER_ATOM_FORCE * n / (f_ms * 1e-3) / 1e9
+                                                            if f_ms > 0 else None),
                                           "peak_GBps": peak, "peak_source": kind},
                         "k_pre": {"avg_ms_incl_rebuilds": p_ms, "bytes_per_atom_no_rebuild": pre_bytes,
-                                  "achieved_GBps": pre_bytes * n / (p_ms * 1e-3) / 1e9, "peak_GBps": peak}}}
+                                  "achieved_GBps": pre_bytes * n / (p_ms * 1e-3) / 1e9 if p_ms > 0 else None,
+                                  "peak_GBps": peak}}}
+    if phases:
+        line["k_pre_phases_us"] = phases
     print(json.dumps(line), flush=True)
 
 

@@ -90,19 +90,31 @@ __device__ __forceinline__ void grid_barrier(const Dev& d) {
 
 // Deterministic block sum of NV doubles (fixed shuffle tree, fixed warp order).
 // Result valid in thread 0.
+// Warp stage: a reduce-scatter butterfly -- at offsets 16, 8, ... each lane
+// keeps half of its values and adds the partner's copy of that half, so after
+// log2(NV) stages lane L holds one value index (bits of L) and the remaining
+// offsets finish plain sums: NV - 1 + log2(32/NV) FP64 adds per lane instead
+// of 5 NV (the FP64 pipe is narrow on GB300).  NV is a power of two <= 32.
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* sm) {
+    static_assert(NV >= 1 && NV <= 32 && (NV & (NV - 1)) == 0, "power of two");
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int idx = 0;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
+    for (int c = NV, o = 16; c > 1; c >>= 1, o >>= 1) {
+        const bool hb = (lane & o) != 0;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+        for (int k = 0; k < c / 2; ++k) {
+            const double send = hb ? v[k] : v[c / 2 + k];
+            const double keep = hb ? v[c / 2 + k] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+        if (hb) idx += c / 2;
     }
+#pragma unroll
+    for (int o = 16 / NV; o > 0; o >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
     __syncthreads();
-    if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) sm[k * 32 + w] = v[k];
-    }
+    if ((lane & (32 / NV - 1)) == 0) sm[idx * 32 + w] = v[0];
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -294,6 +306,42 @@ __device__ void phase_finalize2(const Dev& d, const StepParams& sp, bool couplin
             const double P = (p1 + (-R.virsum) * 0.5) / volume / 3.0;
             W->thermal = th; W->T = T; W->P = P;
             if (coupling) coupling_factors(W, R, T, P, sp.dt);
+        }
+    }
+}
+
+// Mixed path, coupled steps: one pass.  sum_i |v_i - vcm|^2 = sum |v_i|^2 -
+// n |vcm|^2 (as sum v_i = n vcm), so pass 2 and its barriers fold into the
+// finalize of pass 1; then what phase_finalize2 does (box, T, P, coupling).
+// The FP64 path keeps the reference's explicit second pass.
+__device__ void phase_finalize_single(const Dev& d, const StepParams& sp, int sel) {
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const double m = d.mass[sel];
+    for (int r = gw; r < d.nrep; r += warps) {
+        const RepDev R = load_rep(d.rep + r);
+        double S[7];
+        for (int k = 0; k < 7; ++k) S[k] = warp_sum_tiles(d, R, k);
+        if ((threadIdx.x & 31) == 0) {
+            RepDev* W = d.rep + r;
+            const double vc[3] = {S[0] / S[3], S[1] / S[3], S[2] / S[3]};
+            W->vcm[0] = vc[0]; W->vcm[1] = vc[1]; W->vcm[2] = vc[2];
+            W->mom[0] = S[0] * m; W->mom[1] = S[1] * m; W->mom[2] = S[2] * m;
+            W->msum = S[3] * m; W->virsum = S[4]; W->ke = 0.5 * (m * S[5]); W->pe = S[6] * 0.5;
+            W->count = (long long)S[3];
+            const double p1 = m * (S[5] - S[3] * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
+            const double th = 0.5 * p1;
+            double box[3] = {R.box[0], R.box[1], R.box[2]};
+            if (R.pending != 1.0) {
+                for (int k = 0; k < d.ntypes; ++k)
+                    for (int a = 0; a < 3; ++a) box[a] *= R.pending;
+                for (int a = 0; a < 3; ++a) { W->box[a] = box[a]; W->cs[a] = box[a] / (double)R.nc[a]; }
+            }
+            const double volume = box[0] * box[1] * box[2];
+            const double T = temperature_of(th, (long long)S[3]);
+            const double P = (p1 + (-S[4]) * 0.5) / volume / 3.0;
+            W->thermal = th; W->T = T; W->P = P;
+            coupling_factors(W, R, T, P, sp.dt);
         }
     }
 }
@@ -805,6 +853,13 @@ __global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
         const int sel = d.last_type;
         if (d.refmode) {
             phase_serial(d, sp, sel, true);
+            grid_barrier(d);
+        } else if (d.mixed) {
+            phase_partials1(d, sel);
+            grid_barrier(d);
+            phase_chunk_sums(d, 7);
+            grid_barrier(d);
+            phase_finalize_single(d, sp, sel);
             grid_barrier(d);
         } else {
             phase_partials1(d, sel);
