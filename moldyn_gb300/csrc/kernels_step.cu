@@ -835,7 +835,9 @@ struct PhaseClock {
 
 __device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp, PhaseClock& clk);
 
-__global__ void __launch_bounds__(TILE) k_pre(Dev d, StepParams sp) {
+// 6 blocks of 128 threads per SM (80 registers): at the default 64 registers
+// the phases spilled (measured: the rebuild's sort phases ran ~1.8x slower).
+__global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
     tile_rep_reset();
     PhaseClock clk(d.trace);
     if (sp.predrifted) {
