@@ -566,3 +566,24 @@ def test_ieee_conversions_match_cuda(tmp_path):
                            os.path.join(root, "tests", "cuda", "conv_check.cu"), "-o", exe])
     out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
+
+
+def test_trace_phases_account_for_the_step_kernel(mdgb):
+    """MDGB_FLAG_TRACE: per-phase device time of the step kernel; launch and
+    rebuild counts match the steps taken and the rebuild statistics."""
+    pos, vel, box = gs.fcc((8, 8, 8), jitter=0.02, seed=31)
+    e = _engine(mdgb, "mixed", trace=True)
+    _upload(e, pos, vel, box)
+    e.compute_forces()
+    e.trace_phases()                      # reset
+    e.reset_stats()
+    e.step(40, 0.005)
+    ph = e.trace_phases()
+    st = e.stats()
+    assert ph["launches"] == 40
+    assert ph["rebuild_launches"] == st.rebuilds
+    assert all(v >= 0.0 for v in ph.values())
+    if st.rebuilds:
+        assert ph["verlet_list"] > 0.0 and ph["gather"] > 0.0
+    assert e.trace_phases()["launches"] == 0  # read-and-reset
+    e.close()

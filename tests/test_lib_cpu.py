@@ -97,3 +97,29 @@ def test_create_without_gpu_fails_loudly(lib):
 def test_status_strings(lib):
     for s in range(10):
         assert lib.mdgb_status_string(s)
+
+
+def test_splat_rejects_bad_arguments_without_touching_a_gpu(lib):
+    """mdgb_splat validates its arguments before any CUDA call: a camera that
+    is not a symmetric perspective, an empty image or a missing buffer come
+    back as MDGB_ERR_INVALID_ARGUMENT (1), here with no GPU at all."""
+    from moldyn_gb300 import _lib
+    from moldyn_gb300.render import Camera, splat_params
+    parts = np.zeros((2, 12), dtype=np.float32)
+    out = np.zeros((4, 4, 4), dtype=np.float32)
+    prm = splat_params(Camera((0.0, 0.0, 0.0), 70.0, 4, 4))
+    assert lib.mdgb_splat(parts, 2, C.byref(prm), 0, 4, out) == 1
+    assert lib.mdgb_splat(parts, -1, C.byref(prm), 4, 4, out) == 1
+    bad = _lib.CSplatParams()
+    C.memmove(C.byref(bad), C.byref(prm), C.sizeof(prm))
+    bad.proj[11] = 0.0          # not a perspective projection
+    assert lib.mdgb_splat(parts, 2, C.byref(bad), 4, 4, out) == 1
+
+
+def test_trace_flag_and_phase_names():
+    """MDGB_FLAG_TRACE and the phase names mdgb_trace_phases reports."""
+    from moldyn_gb300 import _lib
+    assert _lib.FLAG_TRACE == 8
+    assert len(_lib.TRACE_PHASES) == 14 and _lib.TRACE_PHASES[-2:] == ["launches", "rebuild_launches"]
+    src = open(os.path.join(ROOT, "include", "mdgb.h")).read()
+    assert "#define MDGB_FLAG_TRACE 8u" in src
