@@ -842,7 +842,24 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
     PhaseClock clk(d.trace);
     if (sp.predrifted) {
         // the fused force pass of the previous step kicked and drifted (NVE
-        // chunks): decide, then rebuild or return
+        // chunks).  Every block evaluates the rebuild test of every replica
+        // (same inputs, same answer); when no replica needs one -- most
+        // steps -- block 0 does the bookkeeping and all return without a
+        // grid barrier.
+        bool any = false;
+        for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) any |= rebuild_needed_at(d, sp, d.rep + r);
+        if (!__syncthreads_or(any)) {
+            if (blockIdx.x == 0) {
+                for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) {
+                    RepDev* W = d.rep + r;
+                    W->pending = W->baro_on ? W->myu : 1.0;
+                    W->steps_since = W->steps_since + 1;
+                    W->rebuild = 0;
+                }
+            }
+            clk.mark(TR_DECIDE);
+            return;
+        }
         phase_decide(d, sp);
         grid_barrier(d);
         clk.mark(TR_DECIDE);

@@ -366,6 +366,24 @@ __device__ __forceinline__ RepDev load_rep(const RepDev* p) {
 // after a box scale sc and displacements <= maxd it is at >= sc*rlist -
 // 2*maxd, which must stay above the largest cutoff.  Explicit FP64
 // intrinsics: the step kernel and the fused force pass decide alike.
+__device__ __forceinline__ bool rebuild_needed(const Dev& d, const StepParams& sp, int steps_since0, int rebuild,
+                                               double box0, double box_build0, unsigned max_disp_bits) {
+    const int steps_since = steps_since0 + (sp.do_drift ? 1 : 0);
+    const double sc = __ddiv_rn(box0, box_build0);
+    const double maxd = (double)__uint_as_float(max_disp_bits);
+    const double limit = __dsub_rn(__dsub_rn(__dmul_rn(sc, d.rlist), d.rcmax), __dmul_rn(1e-5, d.rlist));
+    return sp.force_rebuild || rebuild || (__dmul_rn(2.0, maxd) > limit) ||
+           (sp.fixed_interval > 0 && steps_since >= sp.fixed_interval);
+}
+__device__ __forceinline__ bool rebuild_needed(const Dev& d, const StepParams& sp, const RepDev& R) {
+    return rebuild_needed(d, sp, R.steps_since, R.rebuild, R.box[0], R.box_build[0], R.max_disp_bits);
+}
+// the same test reading only the fields it needs (through L2)
+__device__ __forceinline__ bool rebuild_needed_at(const Dev& d, const StepParams& sp, const RepDev* p) {
+    return rebuild_needed(d, sp, __ldcg(&p->steps_since), __ldcg(&p->rebuild), __ldcg(&p->box[0]),
+                          __ldcg(&p->box_build[0]), __ldcg(&p->max_disp_bits));
+}
+
 __device__ __forceinline__ void decide_replica(const Dev& d, const StepParams& sp, int r) {
     const RepDev R = load_rep(d.rep + r);
     RepDev* W = d.rep + r;
@@ -374,11 +392,7 @@ __device__ __forceinline__ void decide_replica(const Dev& d, const StepParams& s
         W->pending = R.baro_on ? R.myu : 1.0;
         ++steps_since;
     }
-    const double sc = __ddiv_rn(R.box[0], R.box_build[0]);
-    const double maxd = (double)__uint_as_float(R.max_disp_bits);
-    const double limit = __dsub_rn(__dsub_rn(__dmul_rn(sc, d.rlist), d.rcmax), __dmul_rn(1e-5, d.rlist));
-    const bool need = sp.force_rebuild || R.rebuild || (__dmul_rn(2.0, maxd) > limit) ||
-                      (sp.fixed_interval > 0 && steps_since >= sp.fixed_interval);
+    const bool need = rebuild_needed(d, sp, R);
     if (need) {
         long long nc[3];
         bool brute = R.cell_cap < 27;
