@@ -311,7 +311,8 @@ def run_ours(args):
         return
 
     # ---- end to end through the C ABI with host buffers -------------------
-    eng = Engine(precision="mixed", skin=SKIN, threads_per_atom=st.threads_per_atom, device=local)
+    eng = Engine(precision="mixed", skin=SKIN, threads_per_atom=st.threads_per_atom, device=local,
+                 graph_steps=max(args.graph_steps, 0))
     eng.set_potential(0, 0, 1.0, 1.0)
     eng.upload(types, pos, vel, [1.0], box)       # warm the allocation path
     eng.compute_forces()
@@ -325,12 +326,25 @@ def run_ours(args):
     out = eng.download()
     t_e2e = max_over_ranks(time.perf_counter() - t0)
     e2e_launches = eng.stats().kernel_launches
+    # the reference's solve loop with --frames-per-save 1: one step, then the
+    # whole state back to the host, every step
+    kf = max(3, min(args.steps, 50))
+    eng.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(kf):
+        eng.step(1, DT)
+        eng.download()
+    t_frames = max_over_ranks(time.perf_counter() - t0)
     eng.close()
     h2d = n * (3 * 8 + 3 * 8 + 2 + 2 * 4)       # positions, velocities, types, (type, rank) staging
     d2h = n * (3 * 8 * 3 + 8 + 8)               # positions, velocities, forces, potential, temp
     e2e = {"value": world * n * args.steps / t_e2e, "unit": "atom-steps/s",
            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-           "includes": "upload + initial forces + K steps + download, wall clock"}
+           "includes": "upload + initial forces + K steps + download, wall clock",
+           "every_step_download": {"value": world * n * kf / t_frames, "unit": "atom-steps/s", "steps": kf,
+                                   "d2h_bytes_per_step": d2h,
+                                   "includes": "per step: one step, then the full state to host buffers"}}
 
     # ---- plain FP64 GPU path ---------------------------------------------
     k64 = max(3, min(args.steps, args.fp64_steps))

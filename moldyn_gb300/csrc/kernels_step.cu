@@ -435,14 +435,45 @@ __device__ void phase_kick(const Dev& d, const StepParams& sp) {
     }
 }
 
+// Inputs of one atom's drift, loaded one tile ahead (the loop is latency-
+// bound: a block walks its tiles one after another).
+struct DriftIn {
+    double4_32a p;
+    double v[3], f[3];
+    int cell;
+    float4 m0;
+};
+
+__device__ __forceinline__ void drift_load(const Dev& d, int s, bool kicked, DriftIn& in) {
+    const int N = d.ntot;
+    in.p = d.pos[s];
+    for (int a = 0; a < 3; ++a) in.v[a] = __ldcg(d.vel + (size_t)a * N + s);
+    if (!kicked)
+        for (int a = 0; a < 3; ++a) in.f[a] = __ldcg(d.frc + (size_t)a * N + s);
+    in.cell = d.cell[s];
+    in.m0 = d.mir0[s];
+}
+
 __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
     __shared__ float smx[32];
     __shared__ float tc[7];   // box (FP32), half box, scale since the last rebuild
     const int N = d.ntot;
+    const bool fm = d.mixed != 0;
     int tc_rep = -1;          // replica tc[] and disp belong to (block-uniform)
     float disp = 0.f;         // largest displacement seen by this thread in replica tc_rep
-    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
-        const int4 tl = d.tiles[t];
+    int t = blockIdx.x;
+    int4 tl = t < d.ntiles ? d.tiles[t] : make_int4(0, 0, 0, 0);
+    DriftIn cur;
+    if (t < d.ntiles && (int)threadIdx.x < tl.z) drift_load(d, tl.y + threadIdx.x, kicked, cur);
+    for (; t < d.ntiles; t += gridDim.x) {
+        // the next tile's inputs in flight while this one computes
+        const int tn = t + gridDim.x;
+        int4 tln = make_int4(0, 0, 0, 0);
+        DriftIn nxt;
+        if (tn < d.ntiles) {
+            tln = d.tiles[tn];
+            if ((int)threadIdx.x < tln.z) drift_load(d, tln.y + threadIdx.x, kicked, nxt);
+        }
         if (tl.x != tc_rep) {
             if (tc_rep >= 0) {
                 const float m = block_max(disp, smx);
@@ -459,18 +490,15 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
         }
         const int s = tl.y + threadIdx.x;
         if ((int)threadIdx.x < tl.z) {
-            double4_32a p = d.pos[s];
+            double4_32a p = cur.p;
             if (sp.do_drift) {
                 const int ty = type_of(p);
                 const double c = sp.kick_c[ty];
-                double vx, vy, vz;
-                if (kicked) {
-                    vx = __ldcg(d.vel + s); vy = __ldcg(d.vel + N + s); vz = __ldcg(d.vel + 2 * N + s);
-                } else {
-                    vx = d.vel[s]; vy = d.vel[N + s]; vz = d.vel[2 * N + s];
-                    vx = madd(vx, d.frc[s], c, d.mixed != 0);           // :30-36 kick
-                    vy = madd(vy, d.frc[N + s], c, d.mixed != 0);
-                    vz = madd(vz, d.frc[2 * N + s], c, d.mixed != 0);
+                double vx = cur.v[0], vy = cur.v[1], vz = cur.v[2];
+                if (!kicked) {
+                    vx = madd(vx, cur.f[0], c, fm);                      // :30-36 kick
+                    vy = madd(vy, cur.f[1], c, fm);
+                    vz = madd(vz, cur.f[2], c, fm);
                 }
                 if (R.thermo_on) {                                       // thermostat.rs:54-58
                     vx = __dmul_rn(vx, R.lambda); vy = __dmul_rn(vy, R.lambda);
@@ -483,18 +511,20 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
                     z = __dmul_rn(z, R.pending);
                 }
                 p.x = x; p.y = y; p.z = z;
-                p = drift_wrap(p, vx, vy, vz, sp.dt, R.box, d.mixed != 0);             // :42-46 drift
+                p = drift_wrap(p, vx, vy, vz, sp.dt, R.box, fm);         // :42-46 drift
                 d.pos[s] = p;
             }
-            const int cl = d.cell[s] - R.cell_base;
+            const int cl = cur.cell - R.cell_base;
             // cl is out of range only before the first binning (fresh upload);
             // the forced rebuild that follows computes the mirror then.
             if (cl >= 0 && cl < R.nc[0] * R.nc[1] * R.nc[2]) {
-                const float4 m = mirror_of(p, cl, R, tc + 3, d.mixed != 0);
+                const float4 m = mirror_of(p, cl, R, tc + 3, fm);
                 d.mir[s] = m;
-                disp = fmaxf(disp, mirror_disp(m, d.mir0[s], tc));
+                disp = fmaxf(disp, mirror_disp(m, cur.m0, tc));
             }
         }
+        tl = tln;
+        cur = nxt;
     }
     if (tc_rep >= 0) {
         const float m = block_max(disp, smx);
