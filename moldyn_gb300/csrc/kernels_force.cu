@@ -527,13 +527,33 @@ __global__ void __launch_bounds__(128) k_force_band(Dev d, StepParams sp, int ki
         const float4 xi = d.mir[s];
         const int ty = type_of(xi);
         const int n = d.nn[s];
+        if (kick && lane == 0) {   // the epilogue's operands, on their way
+            prefetch_l2(d.vel + s);
+            prefetch_l2(d.vel + N + s);
+            prefetch_l2(d.vel + 2 * N + s);
+            if (sp.fused) {
+                prefetch_l2(d.pos + s);
+                prefetch_l2(d.mir0 + s);
+                prefetch_l2(d.cell + s);
+            }
+        }
         long long sx = 0, sy = 0, sz = 0;
         float fx = 0.f, fy = 0.f, fz = 0.f, pe = 0.f, vr = 0.f;
         bool over = false;
-        for (int k = lane; k < n; k += 32) {
-            const uint32_t e = __ldcs(d.nbr + list_index(s, k, tpa, rbeg, rn, d.cap));
+        // this lane's list words and neighbour mirrors, all loads issued before
+        // the maths (the warp handles one atom: latency is the whole cost)
+        constexpr int KB = 4;
+        uint32_t eb[KB];
+        float4 xb[KB];
+#pragma unroll
+        for (int q = 0; q < KB; ++q) {
+            const int k = lane + 32 * q;
+            eb[q] = k < n ? __ldcs(d.nbr + list_index(s, k, tpa, rbeg, rn, d.cap)) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < KB; ++q) xb[q] = __ldg(d.mir + (eb[q] & IDX_MASK));
+        auto entry = [&](uint32_t e, float4 xj) {
             const int j = (int)(e & IDX_MASK);
-            const float4 xj = __ldg(d.mir + j);
             const int c = (int)(e >> IDX_BITS);
             // the shift table of the main kernel (shift_table)
             const float shx = (float)(c % 3 - 1) * csf[0], shy = (float)((c / 3) % 3 - 1) * csf[1],
@@ -543,10 +563,10 @@ __global__ void __launch_bounds__(128) k_force_band(Dev d, StepParams sp, int ki
             const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(xj)];
             const PairF P = pairf(PD);
             const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            if (r2 > P.rc2_hi) continue;
+            if (r2 > P.rc2_hi) return;
             float rr2 = r2;
             if (r2 >= P.rc2_lo) {
-                if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
+                if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) return;
                 rr2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             }
             float fs, u;
@@ -562,6 +582,13 @@ __global__ void __launch_bounds__(128) k_force_band(Dev d, StepParams sp, int ki
                 sy += __float2ll_rn(dy * g);
                 sz += __float2ll_rn(dz * g);
             }
+        };
+#pragma unroll
+        for (int q = 0; q < KB; ++q)
+            if (lane + 32 * q < n) entry(eb[q], xb[q]);
+        for (int k = lane + 32 * KB; k < n; k += 32) {
+            const uint32_t e = __ldcs(d.nbr + list_index(s, k, tpa, rbeg, rn, d.cap));
+            entry(e, __ldg(d.mir + (e & IDX_MASK)));
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
