@@ -15,13 +15,15 @@
 // k_force_mixed -- the chosen path.  FP32 pair maths from the float4 mirror
 //   (cell-relative coordinates, periodic cell shift from the list entry),
 //   force sums in deterministic 64-bit fixed point, potential/virial in FP32
-//   per atom (FP64 across atoms).  Pairs whose FP32 r^2 lies within 1e-5 of
-//   r_cut^2 are re-decided with the reference's FP64 arithmetic, so the set
-//   of interacting pairs equals the reference's.
+//   per atom (FP64 across atoms).  An atom with a pair whose FP32 r^2 lies
+//   within 1e-5 of r_cut^2 is left whole to k_force_band, which decides those
+//   pairs with the reference's FP64 arithmetic, so the set of interacting
+//   pairs equals the reference's.
 //
 // Both end with the second half kick v += F dt/2m (integrator.rs:49-55) when
-// called from a step.  TPA threads share one atom's list; their partial sums
-// are combined by a fixed shuffle tree.
+// called from a step, and on NVE chunks with the next step's first kick and
+// drift (kick_and_drift).  TPA threads share one atom's list; their partial
+// sums are combined by a fixed shuffle tree.
 #include "mdgb_internal.cuh"
 
 namespace mdgb {

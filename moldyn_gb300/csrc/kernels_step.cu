@@ -10,7 +10,15 @@
 //   [rebuild]   per replica, only when the displacement (or a forced rebuild)
 //               asks for it: integer counting sort of atoms into cells
 //               (count -> exclusive scan -> scatter -> canonical order inside
-//               each cell) and the Verlet neighbour list with skin.
+//               each cell); the Verlet list of brute-mode replicas here, of
+//               cell-mode replicas in k_build_list (kernels_list.cu), which
+//               follows every k_pre launch.
+//   After a force pass that already kicked and drifted (NVE chunks), k_pre
+//   only takes the rebuild decision -- without a grid barrier when no replica
+//   needs one -- and rebuilds if needed.
+//
+// On the mixed path the FP64 integration uses fused multiply-adds (explicit
+// __fma_rn); the FP64 path keeps the reference's separate multiply and add.
 //
 // Phases are separated by a bounded grid barrier (the kernel is launched
 // cooperatively, so every block is resident).  A barrier that waits longer
@@ -21,7 +29,7 @@
 //
 // This file is compiled with -fmad=false: its FP64 arithmetic (kick, drift,
 // wrap, reductions, coupling factors) keeps the reference's unfused
-// multiply-then-add rounding.
+// multiply-then-add rounding unless a fused operation is written out.
 #include "mdgb_internal.cuh"
 
 namespace mdgb {
@@ -778,7 +786,7 @@ __device__ void phase_build_list(const Dev& d) {
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
         const RepDev& R = tile_rep(d, tl.x);
-        if (!R.rebuild || R.mode == MODE_CELLS) continue;  // cell-mode replicas: phase_build_list_cells
+        if (!R.rebuild || R.mode == MODE_CELLS) continue;  // cell-mode replicas: k_build_list
         const int s = tl.y + threadIdx.x;
         const int tpa = R.tpa;
         int cnt = 0;
