@@ -1,11 +1,15 @@
 // engine.cu -- host side of libmdgb: the C ABI declared in include/mdgb.h.
 //
-// Drives the kernels of kernels_step.cu / kernels_force.cu on one CUDA
-// stream per handle.  One integrator step (integrator.rs:14-59) is two
-// launches:
-//   k_pre   (cooperative)  coupling reductions -> kick/drift/wrap -> rebuild check
-//                          -> [cell sort + Verlet list, only if needed]
-//   k_force                LJ forces + second half kick
+// Drives the kernels of kernels_step.cu / kernels_list.cu / kernels_force.cu
+// on one CUDA stream per handle.  One integrator step (integrator.rs:14-59)
+// is three or four launches:
+//   k_pre        (cooperative)  coupling reductions -> kick/drift/wrap -> rebuild
+//                               check -> [cell sort, only if needed]
+//   k_build_list                Verlet list of the rebuilt replicas (else returns)
+//   k_force_*                   LJ forces + second half kick (+ on NVE chunks the
+//                               next step's kick and drift, double-buffered)
+//   k_force_band (mixed path)   the atoms with a pair in the FP32-undecidable
+//                               band around r_cut, with FP64 decisions
 // Steps run in chunks; before each chunk the engine snapshots the mutable
 // device state, and if the chunk reports a neighbour-list overflow it grows
 // the list, restores the snapshot and re-runs the chunk -- so capacity
