@@ -37,7 +37,7 @@ __global__ void k_scatter_in(Dev d, const double*, const double*, const int*, co
 __global__ void k_scatter_forces(Dev d, const double*, const double*, const double*);
 __global__ void k_pairs(Dev d, long long capacity, int* out_i, int* out_j, unsigned long long* count);
 using force_fn = void (*)(Dev, StepParams);
-force_fn force_kernel(int tpa, int precision, bool single, bool kick, bool persistent);
+force_fn force_kernel(int tpa, int precision, bool single, bool kick, bool persistent, bool noe);
 using band_fn = void (*)(Dev, StepParams, int);
 band_fn band_kernel(int precision);
 }  // namespace mdgb
@@ -292,7 +292,7 @@ int force_grid(mdgb_engine* e, int c, bool kick) {
     const int ntl = e->class_ntiles[c];
     if (!(e->cfg.flags & MDGB_FLAG_PERSISTENT)) return ntl;
     const int tpa = e->class_tpa[c];
-    force_fn fn = force_kernel(tpa, e->cfg.precision, e->dev.single_type != 0, kick, true);
+    force_fn fn = force_kernel(tpa, e->cfg.precision, e->dev.single_type != 0, kick, true, false);
     int bps = 0;
     if (!fn || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)fn, TILE * tpa, 0) != cudaSuccess)
         bps = 1;
@@ -304,7 +304,8 @@ int force_grid(mdgb_engine* e, int c, bool kick) {
 int launch_force_class(mdgb_engine* e, const StepParams& sp, bool kick, int c) {
     const bool persistent = (e->cfg.flags & MDGB_FLAG_PERSISTENT) != 0;
     const int tpa = e->class_tpa[c];
-    force_fn fn = force_kernel(tpa, e->cfg.precision, e->dev.single_type != 0, kick, persistent);
+    force_fn fn = force_kernel(tpa, e->cfg.precision, e->dev.single_type != 0, kick, persistent,
+                               kick && sp.fused);
     if (!fn) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "threads_per_atom must be 1, 2, 4 or 8");
     Dev d = e->dev;
     d.pos_next = e->pos_alt;

@@ -23,7 +23,9 @@
 // Both end with the second half kick v += F dt/2m (integrator.rs:49-55) when
 // called from a step, and on NVE chunks with the next step's first kick and
 // drift (kick_and_drift).  TPA threads share one atom's list; their partial
-// sums are combined by a fixed shuffle tree.
+// sums are combined by a fixed shuffle tree.  The fused passes of an NVE chunk
+// skip the per-atom potential and virial (NOE): the chunk's last, unfused pass
+// writes them, and nothing reads them in between.
 #include "mdgb_internal.cuh"
 
 namespace mdgb {
@@ -285,7 +287,7 @@ __device__ __forceinline__ void lj_f32(const PairF& P, float r2, float& fs, floa
 
 // NAIVE: the FP32-naive variant of the precision study -- force sums in plain
 // FP32 registers instead of fixed point (same pair maths).
-template <bool NAIVE>
+template <bool NAIVE, bool NOE = false>
 struct MixedAcc {
     FixAcc ax, ay, az;
     float fx, fy, fz;
@@ -299,8 +301,10 @@ struct MixedAcc {
     }
     // fscale_t: the fixed-point scale divided by 2^23; gmax tracks |fs| * fscale_t
     __device__ __forceinline__ void add(f2_t dxy, float dz, float r2, float fs, float u, float fscale_t) {
-        pe += u;
-        vr = fmaf(fs, r2, vr);
+        if (!NOE) {
+            pe += u;
+            vr = fmaf(fs, r2, vr);
+        }
         if (NAIVE) {
             fx = fmaf(f2_lo(dxy), fs, fx); fy = fmaf(f2_hi(dxy), fs, fy); fz = fmaf(dz, fs, fz);
             return;
@@ -327,7 +331,7 @@ __device__ __forceinline__ bool exact_pair(const Dev& d, const RepDev* R, int s,
     return true;
 }
 
-template <int TPA, bool SINGLE, bool KICK, bool PERSIST, bool NAIVE = false>
+template <int TPA, bool SINGLE, bool KICK, bool PERSIST, bool NAIVE = false, bool NOE = false>
 // 9 blocks of 128 threads per SM (56 registers): the kernel is latency-bound
 // on its neighbour gathers, so it keeps as many warps resident as it can.
 __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_force_mixed(Dev d, StepParams sp) {
@@ -369,7 +373,7 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
                 prefetch_l2(d.cell + s);
             }
         }
-        MixedAcc<NAIVE> acc;
+        MixedAcc<NAIVE, NOE> acc;
         acc.init();
         int ty = 0;
         bool deferred = false;   // an atom with a pair in the band goes to k_force_band whole
@@ -485,7 +489,7 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
             } else {
                 sx = tpa_sum_ll<TPA>(sx); sy = tpa_sum_ll<TPA>(sy); sz = tpa_sum_ll<TPA>(sz);
             }
-            pe = tpa_sum_f<TPA>(pe); vr = tpa_sum_f<TPA>(vr);
+            if (!NOE) { pe = tpa_sum_f<TPA>(pe); vr = tpa_sum_f<TPA>(vr); }
         }
         float disp = 0.f;
         if (act && lane == 0 && !deferred) {
@@ -493,7 +497,7 @@ __global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_f
             const double fy = NAIVE ? flt_to_dbl(nfy) : fixed_to_double(sy, d.fscale_log2);
             const double fz = NAIVE ? flt_to_dbl(nfz) : fixed_to_double(sz, d.fscale_log2);
             d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
-            d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr);
+            if (!NOE) { d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr); }
             if (KICK) disp = kick_and_drift(d, sp, R, tcs, s, ty, fx, fy, fz);
         }
         if (KICK && sp.fused) note_displacement(d, tl.x, disp);
@@ -625,7 +629,12 @@ __global__ void __launch_bounds__(128) k_force_band(Dev d, StepParams sp, int ki
 using force_fn = void (*)(Dev, StepParams);
 
 template <int TPA, bool KICK, bool PERSIST>
-static force_fn pick_mixed(bool single, bool naive) {
+static force_fn pick_mixed(bool single, bool naive, bool noe) {
+    if constexpr (KICK) {
+        if (noe && !naive)
+            return single ? (force_fn)k_force_mixed<TPA, true, true, PERSIST, false, true>
+                          : (force_fn)k_force_mixed<TPA, false, true, PERSIST, false, true>;
+    }
     if (naive)
         return single ? (force_fn)k_force_mixed<TPA, true, KICK, PERSIST, true>
                       : (force_fn)k_force_mixed<TPA, false, KICK, PERSIST, true>;
@@ -634,21 +643,22 @@ static force_fn pick_mixed(bool single, bool naive) {
 }
 
 template <int TPA, bool PERSIST>
-static force_fn pick_tpa(int precision, bool single, bool kick) {
+static force_fn pick_tpa(int precision, bool single, bool kick, bool noe) {
     if (precision != 0) {
         const bool naive = precision == 2;
-        return kick ? pick_mixed<TPA, true, PERSIST>(single, naive) : pick_mixed<TPA, false, PERSIST>(single, naive);
+        return kick ? pick_mixed<TPA, true, PERSIST>(single, naive, noe)
+                    : pick_mixed<TPA, false, PERSIST>(single, naive, noe);
     }
     return kick ? (force_fn)k_force_fp64<TPA, true, PERSIST> : (force_fn)k_force_fp64<TPA, false, PERSIST>;
 }
 
 template <bool PERSIST>
-static force_fn pick_persist(int tpa, int precision, bool single, bool kick) {
+static force_fn pick_persist(int tpa, int precision, bool single, bool kick, bool noe) {
     switch (tpa) {
-        case 1: return pick_tpa<1, PERSIST>(precision, single, kick);
-        case 2: return pick_tpa<2, PERSIST>(precision, single, kick);
-        case 4: return pick_tpa<4, PERSIST>(precision, single, kick);
-        case 8: return pick_tpa<8, PERSIST>(precision, single, kick);
+        case 1: return pick_tpa<1, PERSIST>(precision, single, kick, noe);
+        case 2: return pick_tpa<2, PERSIST>(precision, single, kick, noe);
+        case 4: return pick_tpa<4, PERSIST>(precision, single, kick, noe);
+        case 8: return pick_tpa<8, PERSIST>(precision, single, kick, noe);
         default: return nullptr;
     }
 }
@@ -659,9 +669,10 @@ band_fn band_kernel(int precision) {
     return precision == 2 ? (band_fn)k_force_band<true> : (band_fn)k_force_band<false>;
 }
 
-force_fn force_kernel(int tpa, int precision, bool single, bool kick, bool persistent) {
-    return persistent ? pick_persist<true>(tpa, precision, single, kick)
-                      : pick_persist<false>(tpa, precision, single, kick);
+// noe: a fused NVE pass (no per-atom potential/virial); mixed path only.
+force_fn force_kernel(int tpa, int precision, bool single, bool kick, bool persistent, bool noe) {
+    return persistent ? pick_persist<true>(tpa, precision, single, kick, noe)
+                      : pick_persist<false>(tpa, precision, single, kick, noe);
 }
 
 }  // namespace mdgb
