@@ -333,8 +333,11 @@ __device__ __forceinline__ bool exact_pair(const Dev& d, const RepDev* R, int s,
 
 template <int TPA, bool SINGLE, bool KICK, bool PERSIST, bool NAIVE = false, bool NOE = false>
 // 9 blocks of 128 threads per SM (56 registers): the kernel is latency-bound
-// on its neighbour gathers, so it keeps as many warps resident as it can.
-__global__ void __launch_bounds__(TILE * TPA, (9 / TPA) > 0 ? (9 / TPA) : 1) k_force_mixed(Dev d, StepParams sp) {
+// on its neighbour gathers, so it keeps as many warps resident as it can.  The
+// variants that also sum potential and virial need two more registers than
+// that allows (at 56 they spill): 8 blocks, 64 registers.
+__global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE ? 9 : 8) / TPA) : 1)
+    k_force_mixed(Dev d, StepParams sp) {
     __shared__ float4 tab[27];
     __shared__ float tcs[8];
     __shared__ int s_tile;
