@@ -788,10 +788,10 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         (rc = dalloc(e, &d.rep, nrep)) || (rc = dalloc(e, &d.part, 8 * (size_t)e->ntiles)) ||
         (rc = dalloc(e, &d.cpart, 8 * chunks.size())) || (rc = dalloc(e, &d.chunks, chunks.size())) ||
         (rc = dalloc(e, &d.err, 2)) || (rc = dalloc(e, &d.max_needed, 1)) ||
-        (rc = dalloc(e, &d.cell_count, e->ncells)) || (rc = dalloc(e, &d.cell_fill, e->ncells)) ||
+        (rc = dalloc(e, &d.cell_count, e->ncells)) ||
         (rc = dalloc(e, &d.cell_start, e->ncells + 1)) || (rc = dalloc(e, &d.cell_rep, e->ncells)) ||
         (rc = dalloc(e, &d.perm, N)) || (rc = dalloc(e, &d.tmp_pos, N)) ||
-        (rc = dalloc(e, &d.tmp_d, 8 * (size_t)N)) || (rc = dalloc(e, &d.tmp_i, 3 * (size_t)N)) ||
+        (rc = dalloc(e, &d.tmp_d, 8 * (size_t)N)) || (rc = dalloc(e, &d.tmp_i, 4 * (size_t)N)) ||
         (rc = dalloc(e, &d.slot_of_rank, N)) || (rc = dalloc(e, &d.bsum, 4096)) ||
         (rc = dalloc(e, &d.bar, 4)) || (rc = dalloc(e, &d.queue, mdgb_engine::NCLASS)) ||
         (rc = dalloc(e, &e->trace_buf, TR_SLOTS)) ||

@@ -24,8 +24,9 @@
 // called from a step, and on NVE chunks with the next step's first kick and
 // drift (kick_and_drift).  TPA threads share one atom's list; their partial
 // sums are combined by a fixed shuffle tree.  The fused passes of an NVE chunk
-// skip the per-atom potential and virial (NOE): the chunk's last, unfused pass
-// writes them, and nothing reads them in between.
+// (NOE) neither sum the per-atom potential and virial nor store them or the
+// forces (both kicks take the forces from registers): the chunk's last,
+// unfused pass writes all three, and nothing reads them in between.
 #include "mdgb_internal.cuh"
 
 namespace mdgb {
@@ -499,8 +500,10 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
             const double fx = NAIVE ? flt_to_dbl(nfx) : fixed_to_double(sx, d.fscale_log2);
             const double fy = NAIVE ? flt_to_dbl(nfy) : fixed_to_double(sy, d.fscale_log2);
             const double fz = NAIVE ? flt_to_dbl(nfz) : fixed_to_double(sz, d.fscale_log2);
-            d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
-            if (!NOE) { d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr); }
+            if (!NOE) {
+                d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
+                d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr);
+            }
             if (KICK) disp = kick_and_drift(d, sp, R, tcs, s, ty, fx, fy, fz);
         }
         if (KICK && sp.fused) note_displacement(d, tl.x, disp);

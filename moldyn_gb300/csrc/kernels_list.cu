@@ -141,13 +141,11 @@ __global__ void __launch_bounds__(LB_WARPS * 32, 10) k_build_list(Dev d) {
                 const int wn = min(LB_WIN, total - w0);
                 const int nq = (wn + 31) >> 5;
                 __syncwarp();
-                for (int k = 0; k < 27; ++k) {
-                    const int ks = __shfl_sync(FULL, nb_start, k);
-                    const int kn = __shfl_sync(FULL, nb_cnt, k);
-                    const int ko = __shfl_sync(FULL, nb_off, k);
-                    const int lo = max(ko, w0), hi = min(ko + kn, w0 + wn);
-                    for (int p = lo + lane; p < hi; p += 32)
-                        cand[p - w0] = (uint32_t)(ks + p - ko) | ((uint32_t)k << IDX_BITS);
+                // lane k < 27 writes neighbour cell k's run of the window
+                if (lane < 27) {
+                    const int lo = max(nb_off, w0), hi = min(nb_off + nb_cnt, w0 + wn);
+                    const uint32_t tag = (uint32_t)lane << IDX_BITS;
+                    for (int p = lo; p < hi; ++p) cand[p - w0] = (uint32_t)(nb_start + p - nb_off) | tag;
                 }
                 __syncwarp();
                 uint32_t e_n = 0u;

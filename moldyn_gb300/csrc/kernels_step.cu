@@ -555,18 +555,24 @@ __device__ void phase_zero_cells(const Dev& d) {
     const int nt = gridDim.x * blockDim.x;
     for (int c = gt; c < d.ncells; c += nt) {
         const int r = d.cell_rep[c];
-        if (__ldcg(&d.rep[r].rebuild)) { d.cell_count[c] = 0; d.cell_fill[c] = 0; }
+        if (__ldcg(&d.rep[r].rebuild)) d.cell_count[c] = 0;
     }
 }
 
+// Cell of every atom, and its slot among the cell's atoms in arrival order
+// (tmp_i row 3): one counter atomic per distinct cell in a warp -- the atoms
+// are mostly still sorted by cell, so a warp covers only a few.
 __device__ void phase_bin(const Dev& d) {
     const int N = d.ntot;
+    const int lane = threadIdx.x & 31;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
         const RepDev& R = tile_rep(d, tl.x);
         if (!R.rebuild) continue;
         const int s = tl.y + threadIdx.x;
-        if ((int)threadIdx.x >= tl.z) continue;
+        const bool act = (int)threadIdx.x < tl.z;
+        const unsigned am = __ballot_sync(0xffffffffu, act);
+        if (!act) continue;
         const double4_32a p = d.pos[s];
         int local = 0;
         if (R.mode == MODE_CELLS) {
@@ -581,7 +587,12 @@ __device__ void phase_bin(const Dev& d) {
         }
         const int cell = R.cell_base + local;
         d.tmp_i[2 * (size_t)N + s] = cell;
-        atomicAdd(d.cell_count + cell, 1);
+        const unsigned peers = __match_any_sync(am, cell);
+        const int leader = __ffs(peers) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(d.cell_count + cell, __popc(peers));
+        base = __shfl_sync(am, base, leader);
+        d.tmp_i[3 * (size_t)N + s] = base + __popc(peers & ((1u << lane) - 1u));
     }
 }
 
@@ -663,8 +674,7 @@ __device__ void phase_scatter(const Dev& d, bool carry_forces) {
         const int cell = d.tmp_i[2 * (size_t)N + s];
         if (cell < R.cell_base || cell >= R.cell_base + R.cell_cap) { atomicOr(d.err, E_CELLS); continue; }
         // brute mode: one cell holds the whole replica in its current order
-        const int slot = R.mode == MODE_BRUTE ? s
-                                               : __ldcg(d.cell_start + cell) + atomicAdd(d.cell_fill + cell, 1);
+        const int slot = R.mode == MODE_BRUTE ? s : __ldcg(d.cell_start + cell) + d.tmp_i[3 * (size_t)N + s];
         if (slot < R.begin || slot >= R.begin + R.n) { atomicOr(d.err, E_CELLS); continue; }
         d.perm[slot] = s;
         d.tmp_pos[s] = d.pos[s];

@@ -132,13 +132,12 @@ struct Dev {
     int* max_needed;   // largest neighbour count requested
     // rebuild scratch
     int* cell_count;
-    int* cell_fill;
     int* cell_start;   // [ncells+1]
     int* cell_rep;     // replica of each cell
     int* perm;
     double4_32a* tmp_pos;
     double* tmp_d;     // [8][N]: vel3, frc3, epot, evir
-    int* tmp_i;        // [3][N]: orig, rank, cell
+    int* tmp_i;        // [4][N]: orig, rank, cell, slot within the cell
     int* slot_of_rank;
     int* bsum;         // [grid] scan block sums
     unsigned int* bar; // [4] grid barrier: count, generation, any_rebuild, pad
