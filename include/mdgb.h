@@ -220,8 +220,9 @@ MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out);
 /* With MDGB_FLAG_TRACE: microseconds spent in each phase of the per-step
  * kernel since the last call (then reset), in this order: coupling
  * reductions, kick/drift, rebuild decision, then (rebuild launches only) zero
- * cells, bin, scan A, scan B, scan C, scatter, in-cell sort, gather, Verlet
- * list; then the number of step-kernel launches and of rebuild launches.
+ * cells, bin, scan A, scan B, scan C, scatter, in-cell sort (0: the sort runs
+ * inside the gather phase), gather, Verlet list; then the number of
+ * step-kernel launches and of rebuild launches.
  * Writes min(n, 14) values. */
 MDGB_API int mdgb_trace_phases(mdgb_engine* e, double* out, int n);
 MDGB_API int mdgb_reset_stats(mdgb_engine* e);

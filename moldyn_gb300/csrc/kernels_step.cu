@@ -689,99 +689,130 @@ __device__ void phase_scatter(const Dev& d, bool carry_forces) {
     }
 }
 
-// Canonical order inside each cell: ascending caller index.  One warp per
-// cell; every element's rank is the number of smaller keys (keys are distinct
-// caller indices), found by shuffling the cell's keys across the warp.  Cells
-// of brute-mode replicas are already in canonical (identity) order.
+// Canonical order inside each cell (ascending caller index), and every atom
+// moved from the scratch copy to its final slot.  One warp per cell: an
+// element's rank is the number of smaller keys (keys are distinct caller
+// indices), found by shuffling the cell's keys across the warp; the warp then
+// gathers the cell's atoms to cell_start + rank.  Cells of brute-mode
+// replicas are already in canonical (identity) order.
+// carry_forces: also move frc/epot/evir (a refresh that no force evaluation
+// follows).
 constexpr int SORT_MAX_PER_LANE = 4;
 
-__device__ void phase_sort_cells(const Dev& d) {
+// The geometry of one replica that the gather needs, read through L2 (the
+// decide phase of this launch may have changed the box).
+struct CellGeom {
+    double box[3], cs[3];
+    float hL[3];
+    int nc[3];
+    int cell_base, mode, n, r;
+    long long begin;
+};
+
+__device__ __forceinline__ void load_geom(const Dev& d, int r, CellGeom& g) {
+    const RepDev* W = d.rep + r;
+    for (int a = 0; a < 3; ++a) {
+        g.box[a] = __ldcg(&W->box[a]);
+        g.cs[a] = __ldcg(&W->cs[a]);
+        g.nc[a] = __ldcg(&W->nc[a]);
+        g.hL[a] = 0.5f * dbl_to_flt_rn(g.box[a]);
+    }
+    g.cell_base = __ldcg(&W->cell_base);
+    g.mode = __ldcg(&W->mode);
+    g.n = __ldcg(&W->n);
+    g.begin = __ldcg(&W->begin);
+    g.r = r;
+}
+
+// Scratch element i (the atom's index before the rebuild) to slot s of cell c.
+__device__ __forceinline__ void gather_one(const Dev& d, const CellGeom& g, int c, int i, int s,
+                                           bool carry_forces) {
+    const int N = d.ntot;
+    if (i < g.begin || i >= g.begin + g.n || s < g.begin || s >= g.begin + g.n) {
+        atomicOr(d.err, E_BOUNDS);
+        return;
+    }
+    const double4_32a p = ldcg4(d.tmp_pos + i);
+    d.pos[s] = p;
+    for (int k = 0; k < 3; ++k) d.vel[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)k * N + i);
+    if (carry_forces) {
+        for (int k = 0; k < 3; ++k) d.frc[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)(3 + k) * N + i);
+        d.epot[s] = __ldcg(d.tmp_d + (size_t)6 * N + i);
+        d.evir[s] = __ldcg(d.tmp_d + (size_t)7 * N + i);
+    }
+    d.orig[s] = __ldcg(d.tmp_i + i);
+    const int rk = __ldcg(d.tmp_i + (size_t)N + i);
+    d.rank[s] = rk;
+    d.cell[s] = c;
+    const float4 m = mirror_of(p, c - g.cell_base, g, g.hL, d.mixed != 0);
+    d.mir[s] = m;
+    d.mir0[s] = m;
+    if (rk >= 0 && rk < N) d.slot_of_rank[rk] = s;
+    else atomicOr(d.err, E_BOUNDS);
+}
+
+__device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
     const int N = d.ntot;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    CellGeom g;
+    g.r = -1;
     for (int c = gw; c < d.ncells; c += nw) {
         const int r = d.cell_rep[c];
-        if (!__ldcg(&d.rep[r].rebuild) || __ldcg(&d.rep[r].mode) == MODE_BRUTE) continue;
+        if (!__ldcg(&d.rep[r].rebuild)) continue;
         const int b = __ldcg(d.cell_start + c), n = __ldcg(d.cell_count + c);
-        if (n <= 1) continue;
+        if (n <= 0) continue;
         if (b < 0 || b + n > N) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
-        if (n <= 32 * SORT_MAX_PER_LANE) {
+        if (r != g.r) load_geom(d, r, g);
+        if (g.mode == MODE_BRUTE) {
+            // the scatter kept the replica's order: slot i holds element i
+            for (int k = lane; k < n; k += 32) gather_one(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
+        } else if (n <= 32 * SORT_MAX_PER_LANE) {
             int e[SORT_MAX_PER_LANE], key[SORT_MAX_PER_LANE], rank[SORT_MAX_PER_LANE];
 #pragma unroll
-            for (int g = 0; g < SORT_MAX_PER_LANE; ++g) {
-                const int i = g * 32 + lane;
-                e[g] = i < n ? __ldcg(d.perm + b + i) : -1;
-                const bool ok = e[g] >= 0 && e[g] < N;
+            for (int q = 0; q < SORT_MAX_PER_LANE; ++q) {
+                const int i = q * 32 + lane;
+                e[q] = i < n ? __ldcg(d.perm + b + i) : -1;
+                const bool ok = e[q] >= 0 && e[q] < N;
                 if (i < n && !ok) atomicOr(d.err, E_BOUNDS);
-                key[g] = ok ? __ldcg(d.tmp_i + e[g]) : 0x7FFFFFFF;
-                rank[g] = 0;
+                key[q] = ok ? __ldcg(d.tmp_i + e[q]) : 0x7FFFFFFF;
+                rank[q] = 0;
             }
 #pragma unroll
-            for (int g2 = 0; g2 < SORT_MAX_PER_LANE; ++g2) {
-                if (g2 * 32 >= n) break;
+            for (int q2 = 0; q2 < SORT_MAX_PER_LANE; ++q2) {
+                if (q2 * 32 >= n) break;
                 for (int k = 0; k < 32; ++k) {
-                    const int kk = __shfl_sync(0xffffffffu, key[g2], k);
+                    const int kk = __shfl_sync(0xffffffffu, key[q2], k);
 #pragma unroll
-                    for (int g = 0; g < SORT_MAX_PER_LANE; ++g) rank[g] += (kk < key[g]) ? 1 : 0;
+                    for (int q = 0; q < SORT_MAX_PER_LANE; ++q) rank[q] += (kk < key[q]) ? 1 : 0;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < SORT_MAX_PER_LANE; ++q) {
+                const int i = q * 32 + lane;
+                if (i < n && e[q] >= 0 && e[q] < N && rank[q] < n) gather_one(d, g, c, e[q], b + rank[q], carry_forces);
+            }
+        } else {
+            // very crowded cell: serial insertion sort of the slots, then the gather
+            if (lane == 0) {
+                for (int a = 1; a < n; ++a) {
+                    const int e0 = __ldcg(d.perm + b + a);
+                    if (e0 < 0 || e0 >= N) { atomicOr(d.err, E_BOUNDS); break; }
+                    const int k0 = __ldcg(d.tmp_i + e0);
+                    int k = a - 1;
+                    while (k >= 0) {
+                        const int f = __ldcg(d.perm + b + k);
+                        if (f < 0 || f >= N || __ldcg(d.tmp_i + f) <= k0) break;
+                        d.perm[b + k + 1] = f;
+                        --k;
+                    }
+                    d.perm[b + k + 1] = e0;
                 }
             }
             __syncwarp();
-#pragma unroll
-            for (int g = 0; g < SORT_MAX_PER_LANE; ++g) {
-                const int i = g * 32 + lane;
-                if (i < n && rank[g] < n) d.perm[b + rank[g]] = e[g];
-            }
-            __syncwarp();
-        } else if (lane == 0) {
-            // very crowded cell: serial insertion sort
-            for (int a = 1; a < n; ++a) {
-                const int e0 = __ldcg(d.perm + b + a);
-                if (e0 < 0 || e0 >= N) { atomicOr(d.err, E_BOUNDS); break; }
-                const int k0 = __ldcg(d.tmp_i + e0);
-                int k = a - 1;
-                while (k >= 0) {
-                    const int f = __ldcg(d.perm + b + k);
-                    if (f < 0 || f >= N || __ldcg(d.tmp_i + f) <= k0) break;
-                    d.perm[b + k + 1] = f;
-                    --k;
-                }
-                d.perm[b + k + 1] = e0;
-            }
+            for (int k = lane; k < n; k += 32) gather_one(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
         }
-    }
-}
-
-__device__ void phase_gather(const Dev& d, bool carry_forces) {
-    const int N = d.ntot;
-    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
-        const int4 tl = d.tiles[t];
-        const RepDev& R = tile_rep(d, tl.x);
-        if (!R.rebuild) continue;
-        const int s = tl.y + threadIdx.x;
-        if ((int)threadIdx.x >= tl.z) continue;
-        const int i = __ldcg(d.perm + s);
-        if (i < R.begin || i >= R.begin + R.n) { atomicOr(d.err, E_BOUNDS); continue; }
-        const double4_32a p = ldcg4(d.tmp_pos + i);
-        d.pos[s] = p;
-        for (int k = 0; k < 3; ++k) d.vel[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)k * N + i);
-        if (carry_forces) {
-            for (int k = 0; k < 3; ++k) d.frc[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)(3 + k) * N + i);
-            d.epot[s] = __ldcg(d.tmp_d + (size_t)6 * N + i);
-            d.evir[s] = __ldcg(d.tmp_d + (size_t)7 * N + i);
-        }
-        d.orig[s] = __ldcg(d.tmp_i + i);
-        const int rk = __ldcg(d.tmp_i + (size_t)N + i);
-        d.rank[s] = rk;
-        const int cell = __ldcg(d.tmp_i + 2 * (size_t)N + i);
-        d.cell[s] = cell;
-        const float hL[3] = {0.5f * dbl_to_flt_rn(R.box[0]), 0.5f * dbl_to_flt_rn(R.box[1]),
-                             0.5f * dbl_to_flt_rn(R.box[2])};
-        const float4 m = mirror_of(p, cell - R.cell_base, R, hL, d.mixed != 0);
-        d.mir[s] = m;
-        d.mir0[s] = m;
-        if (rk >= 0 && rk < N) d.slot_of_rank[rk] = s;
-        else atomicOr(d.err, E_BOUNDS);
     }
 }
 
@@ -1000,10 +1031,7 @@ __device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp
     phase_scatter(d, !sp.do_drift);
     grid_barrier(d);
     clk.mark(TR_SCATTER);
-    phase_sort_cells(d);
-    grid_barrier(d);
-    clk.mark(TR_SORT);
-    phase_gather(d, !sp.do_drift);
+    phase_sort_gather(d, !sp.do_drift);
     grid_barrier(d);
     clk.mark(TR_GATHER);
     if (clk.tr) clk.tr[TR_STAMP] = clk.last;

@@ -152,7 +152,8 @@ struct Dev {
     int* band_count;
 };
 
-// k_pre phases recorded with MDGB_FLAG_TRACE (slot indices)
+// k_pre phases recorded with MDGB_FLAG_TRACE (slot indices; TR_SORT stays 0,
+// the in-cell sort is part of the gather phase)
 enum : int {
     TR_COUPLING = 0, TR_DRIFT, TR_DECIDE, TR_ZERO, TR_BIN, TR_SCAN_A, TR_SCAN_B, TR_SCAN_C,
     TR_SCATTER, TR_SORT, TR_GATHER, TR_LIST, TR_LAUNCHES, TR_REBUILD_LAUNCHES,
@@ -300,7 +301,9 @@ __device__ __forceinline__ double4_32a drift_wrap(double4_32a p, double vx, doub
 // taken to the nearest periodic image (continuous while the atom stays near
 // its cell; in brute mode the "cell" is the whole box, so it is the wrapped
 // position relative to the box centre).  hL: half box in FP32.
-__device__ __forceinline__ float4 mirror_of(double4_32a p, int cell_local, const RepDev& R, const float* hL,
+// G: a replica record or anything else with its nc, cs and box.
+template <class G>
+__device__ __forceinline__ float4 mirror_of(double4_32a p, int cell_local, const G& R, const float* hL,
                                             bool fused) {
     int cx, cy, cz;
     decode_cell(cell_local, R.nc, cx, cy, cz);
