@@ -51,6 +51,9 @@ BYTES_PER_ATOM_FORCE = 4.0 * LIST_CANDIDATES + 16 + 4 + 24 + 16 + 48
 # NVE chunks fuse the next step's kick + drift into the force launch: position
 # read + write 64, frozen cell 4, rebuild mirror 16, mirror write 16.
 BYTES_PER_ATOM_DRIFT = 64 + 4 + 16 + 16
+# ... and those fused launches store neither the forces nor potential + temp
+# (the chunk's last launch does)
+BYTES_PER_ATOM_FUSED_SKIP = 24 + 16
 ENGINE_CHUNK = 64   # steps per chunk of an eager Engine.step (no graph)
 
 
@@ -380,7 +383,8 @@ def run_ours(args):
     err_fp64 = force_errors(f_fp64_end[:rows], f_ref)
 
     peak, peak_kind = measured_peaks()
-    bytes_per_atom = BYTES_PER_ATOM_FORCE + fused_fraction(args.steps) * BYTES_PER_ATOM_DRIFT
+    bytes_per_atom = BYTES_PER_ATOM_FORCE + fused_fraction(args.steps) * (BYTES_PER_ATOM_DRIFT -
+                                                                          BYTES_PER_ATOM_FUSED_SKIP)
     achieved = bytes_per_atom * n / (force_ms_avg * 1e-3) / 1e9
     tpa_traffic = ncu_traffic_per_atom()
     line = {

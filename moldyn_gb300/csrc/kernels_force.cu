@@ -140,11 +140,13 @@ __device__ __forceinline__ int next_tile(const Dev& d, bool persistent, int& ite
 // into the other position/mirror buffers -- the step kernel that follows only
 // decides and rebuilds.  Same operations, in the same order, as the unfused
 // kick and drift.  Returns the displacement since the last rebuild.
+// FM: the mixed path's fused multiply-adds (a compile-time constant).
+template <bool FM>
 __device__ __forceinline__ float kick_and_drift(const Dev& d, const StepParams& sp, const RepDev* R,
                                                 const float* tcs, int s, int ty, double fx, double fy,
                                                 double fz) {
     const int N = d.ntot;
-    const bool fm = d.mixed != 0;
+    constexpr bool fm = FM;
     const double c = sp.kick_c[ty];
     double vx = madd(d.vel[s], fx, c, fm);
     double vy = madd(d.vel[N + s], fy, c, fm);
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(TILE * TPA) k_force_fp64(Dev d, StepParams sp)
         if (act && lane == 0) {
             d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
             d.epot[s] = pe; d.evir[s] = vr;
-            if (KICK) disp = kick_and_drift(d, sp, R, tcs, s, ty, fx, fy, fz);   // integrator.rs:49-55
+            if (KICK) disp = kick_and_drift<false>(d, sp, R, tcs, s, ty, fx, fy, fz);   // integrator.rs:49-55
         }
         if (KICK && sp.fused) note_displacement(d, tl.x, disp);
     }
@@ -504,7 +506,7 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
                 d.frc[s] = fx; d.frc[N + s] = fy; d.frc[2 * N + s] = fz;
                 d.epot[s] = flt_to_dbl(pe); d.evir[s] = flt_to_dbl(vr);
             }
-            if (KICK) disp = kick_and_drift(d, sp, R, tcs, s, ty, fx, fy, fz);
+            if (KICK) disp = kick_and_drift<true>(d, sp, R, tcs, s, ty, fx, fy, fz);
         }
         if (KICK && sp.fused) note_displacement(d, tl.x, disp);
     }
@@ -623,7 +625,7 @@ __global__ void __launch_bounds__(128) k_force_band(Dev d, StepParams sp, int ki
             if (kick) {
                 float tcs[8];
                 drift_consts(*R, tcs);
-                const float disp = kick_and_drift(d, sp, R, tcs, s, ty, Fx, Fy, Fz);
+                const float disp = kick_and_drift<true>(d, sp, R, tcs, s, ty, Fx, Fy, Fz);
                 if (sp.fused && disp > 0.f) atomicMax(&d.rep[sr.y].max_disp_bits, __float_as_uint(disp));
             }
         }

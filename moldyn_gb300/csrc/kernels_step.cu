@@ -430,6 +430,9 @@ __device__ void phase_serial(const Dev& d, const StepParams& sp, int sel, bool c
 // Nose-Hoover steps: the first kick alone (integrator.rs:30-36), so the
 // thermostat can read the temperature between kick and scaling
 // (thermostat.rs:47-52,59-65).
+// FM (here and in the phases below): the mixed path's fused multiply-adds,
+// a compile-time constant -- the callers dispatch on d.mixed once per phase.
+template <bool FM>
 __device__ void phase_kick(const Dev& d, const StepParams& sp) {
     const int N = d.ntot;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
@@ -439,7 +442,7 @@ __device__ void phase_kick(const Dev& d, const StepParams& sp) {
         const int ty = (int)reinterpret_cast<const long long*>(d.pos + s)[3];
         const double c = sp.kick_c[ty];
         for (int a = 0; a < 3; ++a)
-            d.vel[(size_t)a * N + s] = madd(d.vel[(size_t)a * N + s], d.frc[(size_t)a * N + s], c, d.mixed != 0);
+            d.vel[(size_t)a * N + s] = madd(d.vel[(size_t)a * N + s], d.frc[(size_t)a * N + s], c, FM);
     }
 }
 
@@ -462,11 +465,12 @@ __device__ __forceinline__ void drift_load(const Dev& d, int s, bool kicked, Dri
     in.m0 = d.mir0[s];
 }
 
+template <bool FM>
 __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
     __shared__ float smx[32];
     __shared__ float tc[7];   // box (FP32), half box, scale since the last rebuild
     const int N = d.ntot;
-    const bool fm = d.mixed != 0;
+    constexpr bool fm = FM;
     int tc_rep = -1;          // replica tc[] and disp belong to (block-uniform)
     float disp = 0.f;         // largest displacement seen by this thread in replica tc_rep
     int t = blockIdx.x;
@@ -509,14 +513,14 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
                     vz = madd(vz, cur.f[2], c, fm);
                 }
                 if (R.thermo_on) {                                       // thermostat.rs:54-58
-                    vx = __dmul_rn(vx, R.lambda); vy = __dmul_rn(vy, R.lambda);
-                    vz = __dmul_rn(vz, R.lambda);
+                    vx = dmul_nospec(vx, R.lambda); vy = dmul_nospec(vy, R.lambda);
+                    vz = dmul_nospec(vz, R.lambda);
                 }
                 d.vel[s] = vx; d.vel[N + s] = vy; d.vel[2 * N + s] = vz;
                 double x = p.x, y = p.y, z = p.z;
                 if (R.pending != 1.0) {                                  // barostat.rs:46-48
-                    x = __dmul_rn(x, R.pending); y = __dmul_rn(y, R.pending);
-                    z = __dmul_rn(z, R.pending);
+                    x = dmul_nospec(x, R.pending); y = dmul_nospec(y, R.pending);
+                    z = dmul_nospec(z, R.pending);
                 }
                 p.x = x; p.y = y; p.z = z;
                 p = drift_wrap(p, vx, vy, vz, sp.dt, R.box, fm);         // :42-46 drift
@@ -725,6 +729,7 @@ __device__ __forceinline__ void load_geom(const Dev& d, int r, CellGeom& g) {
 }
 
 // Scratch element i (the atom's index before the rebuild) to slot s of cell c.
+template <bool FM>
 __device__ __forceinline__ void gather_one(const Dev& d, const CellGeom& g, int c, int i, int s,
                                            bool carry_forces) {
     const int N = d.ntot;
@@ -744,13 +749,14 @@ __device__ __forceinline__ void gather_one(const Dev& d, const CellGeom& g, int 
     const int rk = __ldcg(d.tmp_i + (size_t)N + i);
     d.rank[s] = rk;
     d.cell[s] = c;
-    const float4 m = mirror_of(p, c - g.cell_base, g, g.hL, d.mixed != 0);
+    const float4 m = mirror_of(p, c - g.cell_base, g, g.hL, FM);
     d.mir[s] = m;
     d.mir0[s] = m;
     if (rk >= 0 && rk < N) d.slot_of_rank[rk] = s;
     else atomicOr(d.err, E_BOUNDS);
 }
 
+template <bool FM>
 __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
     const int N = d.ntot;
     const int lane = threadIdx.x & 31;
@@ -767,7 +773,7 @@ __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
         if (r != g.r) load_geom(d, r, g);
         if (g.mode == MODE_BRUTE) {
             // the scatter kept the replica's order: slot i holds element i
-            for (int k = lane; k < n; k += 32) gather_one(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
+            for (int k = lane; k < n; k += 32) gather_one<FM>(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
         } else if (n <= 32 * SORT_MAX_PER_LANE) {
             int e[SORT_MAX_PER_LANE], key[SORT_MAX_PER_LANE], rank[SORT_MAX_PER_LANE];
 #pragma unroll
@@ -791,7 +797,7 @@ __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
 #pragma unroll
             for (int q = 0; q < SORT_MAX_PER_LANE; ++q) {
                 const int i = q * 32 + lane;
-                if (i < n && e[q] >= 0 && e[q] < N && rank[q] < n) gather_one(d, g, c, e[q], b + rank[q], carry_forces);
+                if (i < n && e[q] >= 0 && e[q] < N && rank[q] < n) gather_one<FM>(d, g, c, e[q], b + rank[q], carry_forces);
             }
         } else {
             // very crowded cell: serial insertion sort of the slots, then the gather
@@ -811,7 +817,7 @@ __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
                 }
             }
             __syncwarp();
-            for (int k = lane; k < n; k += 32) gather_one(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
+            for (int k = lane; k < n; k += 32) gather_one<FM>(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
         }
     }
 }
@@ -977,7 +983,7 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
     }
     if (sp.do_drift && sp.thermo_nh) {
         const int sel = d.last_type;
-        phase_kick(d, sp);
+        if (d.mixed) phase_kick<true>(d, sp); else phase_kick<false>(d, sp);
         grid_barrier(d);
         if (d.refmode) {
             phase_serial(d, sp, sel, false, true);
@@ -996,9 +1002,9 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
             phase_finalize_nh(d, sp, sel);
             grid_barrier(d);
         }
-        phase_drift(d, sp, true);
+        if (d.mixed) phase_drift<true>(d, sp, true); else phase_drift<false>(d, sp, true);
     } else {
-        phase_drift(d, sp, false);
+        if (d.mixed) phase_drift<true>(d, sp, false); else phase_drift<false>(d, sp, false);
     }
     grid_barrier(d);
     clk.mark(TR_DRIFT);
@@ -1031,7 +1037,7 @@ __device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp
     phase_scatter(d, !sp.do_drift);
     grid_barrier(d);
     clk.mark(TR_SCATTER);
-    phase_sort_gather(d, !sp.do_drift);
+    if (d.mixed) phase_sort_gather<true>(d, !sp.do_drift); else phase_sort_gather<false>(d, !sp.do_drift);
     grid_barrier(d);
     clk.mark(TR_GATHER);
     if (clk.tr) clk.tr[TR_STAMP] = clk.last;

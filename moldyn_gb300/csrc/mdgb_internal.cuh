@@ -272,18 +272,36 @@ __device__ __forceinline__ void decode_cell(int l, const int nc[3], int& cx, int
 // translation units (compiled with different contraction settings) produce
 // the same bits.
 
+// x + y and x * y rounded to nearest, for operations under a branch that is
+// rarely or conditionally taken: as volatile inline PTX the compiler cannot
+// evaluate them unconditionally and select the result (which it does with
+// __dadd_rn / __dmul_rn, costing FP64 operations on every call on GB300's
+// narrow FP64 pipe).  Same bits as __dadd_rn / __dmul_rn.
+__device__ __forceinline__ double dadd_nospec(double x, double y) {
+    double r;
+    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(y));
+    return r;
+}
+__device__ __forceinline__ double dmul_nospec(double x, double y) {
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(y));
+    return r;
+}
+
 // core/src/particle.rs:120-141 with the comparisons done on the bit patterns:
 // for x >= 0 and L > 0 the signed 64-bit order of the bits is the numeric
-// order, and x < 0.0 is "sign bit set and not -0.0".
+// order, and x < 0.0 is "sign bit set and not -0.0".  x - L is x + (-L).
 __device__ __forceinline__ double wrap_ref(double x, double L) {
     const long long b = __double_as_longlong(x);
-    if (b < 0 && b != (long long)0x8000000000000000ull) return __dadd_rn(x, L);
-    if (b >= __double_as_longlong(L)) return __dsub_rn(x, L);
+    if (b < 0 && b != (long long)0x8000000000000000ull) return dadd_nospec(x, L);
+    if (b >= __double_as_longlong(L)) return dadd_nospec(x, -L);
     return x;
 }
 
 // a + b * c: the reference's two roundings (FP64 path) or one fused
 // multiply-add (mixed path: half the operations on GB300's narrow FP64 pipe).
+// `fused` must be a compile-time constant at every call (a run-time flag has
+// the compiler evaluate both forms and select).
 __device__ __forceinline__ double madd(double a, double b, double c, bool fused) {
     return fused ? __fma_rn(b, c, a) : __dadd_rn(a, __dmul_rn(b, c));
 }
@@ -320,8 +338,8 @@ __device__ __forceinline__ float4 mirror_of(double4_32a p, int cell_local, const
         // nearest image of the atom relative to its cell centre; only atoms that
         // just crossed the periodic boundary (|u| ~ L) take this branch, far
         // from the +-L/2 decision edge, so the FP32 comparison decides it
-        if (f >= h) { u = __dsub_rn(u, R.box[a]); f = dbl_to_flt_rn(u); }
-        else if (f < -h) { u = __dadd_rn(u, R.box[a]); f = dbl_to_flt_rn(u); }
+        if (f >= h) { u = dadd_nospec(u, -R.box[a]); f = dbl_to_flt_rn(u); }
+        else if (f < -h) { u = dadd_nospec(u, R.box[a]); f = dbl_to_flt_rn(u); }
         o[a] = f;
     }
     return make_float4(o[0], o[1], o[2], __int_as_float(type_of(p)));
