@@ -169,6 +169,17 @@ const LJ& pot_of(const mdgb_engine* e, int a, int b) {
     return e->pot[a][b].set ? e->pot[a][b] : e->pot_default;
 }
 
+// The smallest double t whose correctly rounded square root exceeds rc: for
+// the reference's test sqrt(r^2) <= rc the same as r^2 < t (sqrt is monotonic
+// and IEEE-exact on the host).
+double sqrt_cut(double rc) {
+    if (!(rc > 0.0) || !std::isfinite(rc)) return rc > 0.0 ? INFINITY : 0.0;
+    double t = rc * rc;
+    while (t > 0.0 && std::sqrt(t) > rc) t = std::nextafter(t, 0.0);
+    while (std::sqrt(t) <= rc) t = std::nextafter(t, INFINITY);
+    return t;
+}
+
 int upload_pairs(mdgb_engine* e) {
     std::vector<PairDev> tab(MAX_TYPES * MAX_TYPES);
     double fchar = 0.0;
@@ -187,6 +198,7 @@ int upload_pairs(mdgb_engine* e) {
             const double rc2 = p.rc * p.rc;
             q.rc2f_lo = (float)(rc2 * (1.0 - 1e-5));
             q.rc2f_hi = (float)(rc2 * (1.0 + 1e-5));
+            q.rc2_cut = sqrt_cut(p.rc);
             tab[a * MAX_TYPES + b] = q;
             if (a < e->ntypes && b < e->ntypes) {
                 e->rcmax = std::max(e->rcmax, p.rc);

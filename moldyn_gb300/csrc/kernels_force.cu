@@ -322,14 +322,32 @@ struct MixedAcc {
     }
 };
 
-// The reference's FP64 decision for one pair; on success (dx,dy,dz) is the
-// FP64 displacement rounded to FP32.
-__device__ __forceinline__ bool exact_pair(const Dev& d, const RepDev* R, int s, int j, double rc, float& dx,
-                                           float& dy, float& dz) {
-    const double box[3] = {R->box[0], R->box[1], R->box[2]};
-    double rx, ry, rz;
-    const double r = ref_distance(d.pos[s], d.pos[j], box, rx, ry, rz);
-    if (r > rc) return false;
+// The reference's minimum image of one FP64 displacement component
+// (potential.rs:186-200: r < -L/2 -> r + L, r > L/2 -> r - L) with the
+// comparisons on the bit patterns (L/2 exact: exponent - 1): integer work
+// instead of GB300's narrow FP64 pipe.
+__device__ __forceinline__ double min_image_ref(double r, double L) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(r);
+    const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+    const unsigned long long half = (unsigned long long)__double_as_longlong(L) - (1ull << 52);
+    if (mag > half) return dadd_nospec(r, (b >> 63) ? L : -L);
+    return r;
+}
+
+// The reference's FP64 decision for one pair (potential.rs:181-204: the
+// minimum-image displacement, r = sqrt(r^2), interacting when r <= r_cut);
+// on success (dx,dy,dz) is the FP64 displacement rounded to FP32.  No square
+// root: sqrt_rn(r^2) <= r_cut exactly when r^2 < rc2_cut, the smallest double
+// whose correctly rounded square root exceeds r_cut (computed on the host).
+__device__ __forceinline__ bool exact_pair(const Dev& d, const RepDev* R, int s, int j, const PairDev& PD,
+                                           float& dx, float& dy, float& dz) {
+    const double4_32a pi = d.pos[s], pj = d.pos[j];
+    const double rx = min_image_ref(__dsub_rn(pj.x, pi.x), R->box[0]);
+    const double ry = min_image_ref(__dsub_rn(pj.y, pi.y), R->box[1]);
+    const double rz = min_image_ref(__dsub_rn(pj.z, pi.z), R->box[2]);
+    const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+    // both non-negative: the bit patterns order like the values
+    if (__double_as_longlong(r2) >= __double_as_longlong(PD.rc2_cut)) return false;
     dx = dbl_to_flt_rn(rx); dy = dbl_to_flt_rn(ry); dz = dbl_to_flt_rn(rz);
     return true;
 }
@@ -438,7 +456,7 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
                     const int j = (int)(e & IDX_MASK);
                     const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(__ldg(d.mir + j))];
                     float dx, dy, dz;
-                    if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
+                    if (!exact_pair(d, R, s, j, PD, dx, dy, dz)) continue;
                     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                     float fs, u;
                     lj_f32(pairf(PD), r2, fs, u);
@@ -472,11 +490,11 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
                 const PairDev& PD = d.pair[ty * MAX_TYPES + type_of(xj)];
                 const PairF P = pairf(PD);
                 if (brute) {
-                    if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
+                    if (!exact_pair(d, R, s, j, PD, dx, dy, dz)) continue;
                 } else {
                     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                     if (r2 > P.rc2_hi) continue;
-                    if (r2 >= P.rc2_lo && !exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) continue;
+                    if (r2 >= P.rc2_lo && !exact_pair(d, R, s, j, PD, dx, dy, dz)) continue;
                 }
                 const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                 float fs, u;
@@ -580,7 +598,7 @@ __global__ void __launch_bounds__(128) k_force_band(Dev d, StepParams sp, int ki
             if (r2 > P.rc2_hi) return;
             float rr2 = r2;
             if (r2 >= P.rc2_lo) {
-                if (!exact_pair(d, R, s, j, PD.rc, dx, dy, dz)) return;
+                if (!exact_pair(d, R, s, j, PD, dx, dy, dz)) return;
                 rr2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             }
             float fs, u;

@@ -165,30 +165,54 @@ __device__ __forceinline__ int block_max_int(int v, int* sm) {
 // <= CHUNK_TILES tiles (phase_chunk_sums), then one warp per replica over its
 // chunks -- a replica of millions of atoms is summed by many warps in
 // parallel, always in the same order.
-__device__ void phase_chunk_sums(const Dev& d, int nslots) {
+// Rows of 8 partials (one per tile or chunk, 64 bytes) summed slot by slot by
+// one warp: lane l adds rows l, l + 32, ... in order, then a shuffle tree per
+// slot.  Each lane loads a row's slots together (four 16-byte loads), so the
+// loads of all slots are in flight at once.  Result valid in lane 0.
+template <int NS>
+__device__ __forceinline__ void warp_sum_rows(const double* rows, int n, double (&s)[NS]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) s[k] = 0.0;
+    for (int t = lane; t < n; t += 32) {
+        const double2* row = reinterpret_cast<const double2*>(rows + (size_t)t * 8);
+        double v[8];
+#pragma unroll
+        for (int q = 0; q < (NS + 1) / 2; ++q) {
+            const double2 x = __ldcg(row + q);
+            v[2 * q] = x.x; v[2 * q + 1] = x.y;
+        }
+#pragma unroll
+        for (int k = 0; k < NS; ++k) s[k] += v[k];
+    }
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], off);
+    }
+}
+
+template <int NS>
+__device__ void phase_chunk_sums(const Dev& d) {
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int c = gw; c < d.nchunks; c += nw) {
         const int4 ch = d.chunks[c];
-        for (int k = 0; k < nslots; ++k) {
-            double s = 0.0;
-            for (int t = lane; t < ch.z; t += 32) s += __ldcg(d.part + (size_t)(ch.y + t) * 8 + k);
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-            if (lane == 0) d.cpart[(size_t)c * 8 + k] = s;
-        }
+        double s[NS];
+        warp_sum_rows<NS>(d.part + (size_t)ch.y * 8, ch.z, s);
+        if (lane == 0)
+            for (int k = 0; k < NS; ++k) d.cpart[(size_t)c * 8 + k] = s[k];
     }
 }
 
-// Sum over the chunk partials of one replica by one warp (fixed order).
-__device__ __forceinline__ double warp_sum_tiles(const Dev& d, const RepDev& R, int slot) {
-    const int lane = threadIdx.x & 31;
-    double s = 0.0;
-    for (int c = lane; c < R.nchunks; c += 32) s += __ldcg(d.cpart + (size_t)(R.chunk_begin + c) * 8 + slot);
+// Sums over the chunk partials of one replica by one warp (fixed order),
+// slots 0..NS-1, broadcast to every lane.
+template <int NS>
+__device__ __forceinline__ void warp_sum_tiles(const Dev& d, const RepDev& R, double (&S)[NS]) {
+    warp_sum_rows<NS>(d.cpart + (size_t)R.chunk_begin * 8, R.nchunks, S);
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    return __shfl_sync(0xffffffffu, s, 0);
+    for (int k = 0; k < NS; ++k) S[k] = __shfl_sync(0xffffffffu, S[k], 0);
 }
 
 
@@ -197,27 +221,50 @@ __device__ __forceinline__ double warp_sum_tiles(const Dev& d, const RepDev& R, 
 // factored out of the sums and applied once per replica; halving is exact
 // and applied once too -- fewer FP64-pipe operations per atom).
 // Pass 1 slots: 0-2 sum(v), 3 count, 4 sum(temp), 5 sum(v.v), 6 sum(potential).
+// One atom's inputs of pass 1, loaded a tile ahead (a block walks its tiles
+// one after another; the loads of the next overlap this one's sums).
+struct Pass1In {
+    int ty;
+    double vx, vy, vz, vir, pot;
+};
+
+__device__ __forceinline__ void pass1_load(const Dev& d, int s, Pass1In& in) {
+    const int N = d.ntot;
+    in.ty = (int)__ldcg(reinterpret_cast<const long long*>(d.pos + s) + 3);
+    in.vx = __ldcg(d.vel + s); in.vy = __ldcg(d.vel + N + s); in.vz = __ldcg(d.vel + 2 * N + s);
+    in.vir = __ldcg(d.evir + s);
+    in.pot = __ldcg(d.epot + s);
+}
+
 __device__ void phase_partials1(const Dev& d, int sel) {
     __shared__ double sm[8 * 32];
-    const int N = d.ntot;
-    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
-        const int4 tl = d.tiles[t];
-        const int s = tl.y + threadIdx.x;
+    int t = blockIdx.x;
+    int4 tl = t < d.ntiles ? d.tiles[t] : make_int4(0, 0, 0, 0);
+    Pass1In cur;
+    cur.ty = -1;
+    if (t < d.ntiles && (int)threadIdx.x < tl.z) pass1_load(d, tl.y + threadIdx.x, cur);
+    for (; t < d.ntiles; t += gridDim.x) {
+        const int tn = t + gridDim.x;
+        int4 tln = make_int4(0, 0, 0, 0);
+        Pass1In nxt;
+        nxt.ty = -1;
+        if (tn < d.ntiles) {
+            tln = d.tiles[tn];
+            if ((int)threadIdx.x < tln.z) pass1_load(d, tln.y + threadIdx.x, nxt);
+        }
         double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if ((int)threadIdx.x < tl.z) {
-            const int ty = (int)__ldcg(reinterpret_cast<const long long*>(d.pos + s) + 3);
-            if (ty == sel) {
-                const double vx = __ldcg(d.vel + s), vy = __ldcg(d.vel + N + s),
-                             vz = __ldcg(d.vel + 2 * N + s);
-                v[0] = vx; v[1] = vy; v[2] = vz; v[3] = 1.0;
-                v[4] = __ldcg(d.evir + s);
-                v[5] = vx * vx + vy * vy + vz * vz;
-                v[6] = __ldcg(d.epot + s);
-            }
+        if ((int)threadIdx.x < tl.z && cur.ty == sel) {
+            const double vx = cur.vx, vy = cur.vy, vz = cur.vz;
+            v[0] = vx; v[1] = vy; v[2] = vz; v[3] = 1.0;
+            v[4] = cur.vir;
+            v[5] = vx * vx + vy * vy + vz * vz;
+            v[6] = cur.pot;
         }
         block_sum<8>(v, sm);
         if (threadIdx.x == 0)
             for (int k = 0; k < 8; ++k) d.part[(size_t)t * 8 + k] = v[k];
+        tl = tln;
+        cur = nxt;
     }
 }
 
@@ -229,8 +276,8 @@ __device__ void phase_finalize1(const Dev& d, int sel) {
     const double m = d.mass[sel];
     for (int r = gw; r < d.nrep; r += warps) {
         const RepDev R = load_rep(d.rep + r);
-        double S[8];
-        for (int k = 0; k < 7; ++k) S[k] = warp_sum_tiles(d, R, k);
+        double S[7];
+        warp_sum_tiles<7>(d, R, S);
         if ((threadIdx.x & 31) == 0) {
             RepDev* W = d.rep + r;
             W->vcm[0] = S[0] / S[3]; W->vcm[1] = S[1] / S[3]; W->vcm[2] = S[2] / S[3];
@@ -298,7 +345,9 @@ __device__ void phase_finalize2(const Dev& d, const StepParams& sp, bool couplin
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     for (int r = gw; r < d.nrep; r += warps) {
         const RepDev R = load_rep(d.rep + r);
-        const double sdv = warp_sum_tiles(d, R, 0);
+        double S1[1];
+        warp_sum_tiles<1>(d, R, S1);
+        const double sdv = S1[0];
         const double p1 = d.mass[sel] * sdv;              // sum m |v - vcm|^2 (pressure.rs:13-17)
         const double th = 0.5 * p1;                        // energy.rs:25-37
         if ((threadIdx.x & 31) == 0) {
@@ -329,7 +378,7 @@ __device__ void phase_finalize_single(const Dev& d, const StepParams& sp, int se
     for (int r = gw; r < d.nrep; r += warps) {
         const RepDev R = load_rep(d.rep + r);
         double S[7];
-        for (int k = 0; k < 7; ++k) S[k] = warp_sum_tiles(d, R, k);
+        warp_sum_tiles<7>(d, R, S);
         if ((threadIdx.x & 31) == 0) {
             RepDev* W = d.rep + r;
             const double vc[3] = {S[0] / S[3], S[1] / S[3], S[2] / S[3]};
@@ -367,7 +416,9 @@ __device__ void phase_finalize_nh(const Dev& d, const StepParams& sp, int sel) {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     for (int r = gw; r < d.nrep; r += warps) {
         const RepDev R = load_rep(d.rep + r);
-        const double sdv = warp_sum_tiles(d, R, 0);
+        double S1[1];
+        warp_sum_tiles<1>(d, R, S1);
+        const double sdv = S1[0];
         if ((threadIdx.x & 31) == 0) nh_update_psi(d.rep + r, R, temperature_of(0.5 * (d.mass[sel] * sdv), R.count), sp.dt);
     }
 }
@@ -961,20 +1012,20 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
         } else if (d.mixed) {
             phase_partials1(d, sel);
             grid_barrier(d);
-            phase_chunk_sums(d, 7);
+            phase_chunk_sums<7>(d);
             grid_barrier(d);
             phase_finalize_single(d, sp, sel);
             grid_barrier(d);
         } else {
             phase_partials1(d, sel);
             grid_barrier(d);
-            phase_chunk_sums(d, 7);
+            phase_chunk_sums<7>(d);
             grid_barrier(d);
             phase_finalize1(d, sel);
             grid_barrier(d);
             phase_partials2(d, sel);
             grid_barrier(d);
-            phase_chunk_sums(d, 1);
+            phase_chunk_sums<1>(d);
             grid_barrier(d);
             phase_finalize2(d, sp, true, sel);
             grid_barrier(d);
@@ -991,13 +1042,13 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
         } else {
             phase_partials1(d, sel);
             grid_barrier(d);
-            phase_chunk_sums(d, 7);
+            phase_chunk_sums<7>(d);
             grid_barrier(d);
             phase_finalize1(d, sel);
             grid_barrier(d);
             phase_partials2(d, sel);
             grid_barrier(d);
-            phase_chunk_sums(d, 1);
+            phase_chunk_sums<1>(d);
             grid_barrier(d);
             phase_finalize_nh(d, sp, sel);
             grid_barrier(d);
@@ -1056,13 +1107,13 @@ __global__ void __launch_bounds__(TILE) k_macro(Dev d, StepParams sp, int sel) {
     }
     phase_partials1(d, sel);
     grid_barrier(d);
-    phase_chunk_sums(d, 7);
+    phase_chunk_sums<7>(d);
     grid_barrier(d);
     phase_finalize1(d, sel);
     grid_barrier(d);
     phase_partials2(d, sel);
     grid_barrier(d);
-    phase_chunk_sums(d, 1);
+    phase_chunk_sums<1>(d);
     grid_barrier(d);
     phase_finalize2(d, sp, false, sel);
 }

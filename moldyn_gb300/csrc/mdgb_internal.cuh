@@ -54,6 +54,7 @@ struct PairDev {
     float sig2f, eps4f, eps24f, ucutf;
     float rc2f_lo, rc2f_hi;  // band around rc^2 decided exactly in FP64
     int pad0, pad1;
+    double rc2_cut;          // smallest double whose rounded square root exceeds rc
 };
 
 struct RepDev {
