@@ -485,6 +485,30 @@ def test_fixed_point_overflow_is_reported(mdgb):
     e.close()
 
 
+@pytest.mark.parametrize("kw", [{}, dict(graph_steps=10)])
+def test_nve_chunk_leaves_current_forces_potential_and_temp(mdgb, kw):
+    """The fused passes of an NVE chunk store neither forces nor per-atom
+    potential and temp; the chunk's last pass must leave all three as a fresh
+    evaluation at the final positions gives them.  A fresh engine bins the
+    atoms anew (other cell centres, so other FP32 roundings): compared at the
+    mixed bar, 1e-5 of the rms -- values one step old are off by ~1e-2."""
+    pos, vel, box = gs.fcc((8, 8, 8), jitter=0.04, seed=33)
+    e = _engine(mdgb, "mixed", threads_per_atom=1, **kw)
+    _upload(e, pos, vel, box)
+    e.compute_forces()
+    e.step(30, 0.005)
+    out = e.download()
+    e.close()
+    f = _engine(mdgb, "mixed", threads_per_atom=1)
+    _upload(f, out["pos"], out["vel"], box)
+    f.compute_forces()
+    fresh = f.download()
+    f.close()
+    for k in ("force", "potential", "temp"):
+        scale = np.sqrt(np.mean(fresh[k] ** 2))
+        assert np.max(np.abs(out[k] - fresh[k])) <= 1e-5 * scale, k
+
+
 def test_mixed_is_deterministic(mdgb):
     pos, vel, box = gs.fcc((8, 8, 8), jitter=0.04, seed=31)
     outs = []
