@@ -356,6 +356,7 @@ def run_ours(args):
     eng.upload(types, end["pos"], end["vel"], [1.0], box)
     eng.compute_forces()
     f_fp64_end = eng.download()["force"] if rank == 0 else None
+    mac_fp64 = eng.macro(0)
     eng.step(3, DT)
     eng.synchronize()
     stream64 = torch.cuda.ExternalStream(eng.stream_ptr)
@@ -372,6 +373,21 @@ def run_ours(args):
 
     if rank != 0:
         return
+
+    # the mixed path's macro parameters at the same state (its own forces,
+    # potential and virial) against the FP64 path's
+    em = Engine(precision="mixed", skin=SKIN, device=local)
+    em.set_potential(0, 0, 1.0, 1.0)
+    em.upload(types, end["pos"], end["vel"], [1.0], box)
+    em.compute_forces()
+    mac_mixed = em.macro(0)
+    em.close()
+    macro_err = {k: abs(mac_mixed[k] - mac_fp64[k]) / abs(mac_fp64[k])
+                 for k in ("kinetic_energy", "potential_energy", "thermal_energy", "temperature", "pressure")}
+    e_tot = mac_fp64["kinetic_energy"] + mac_fp64["potential_energy"]
+    macro_err["total_energy"] = abs(mac_mixed["kinetic_energy"] + mac_mixed["potential_energy"] - e_tot) / abs(e_tot)
+    macro_err["definition"] = ("|mixed - fp64| / |fp64| at the end state of the timed run; the FP64 GPU path "
+                               "matches the oracle to ~1e-15 in the parity tests")
 
     # ---- CPU baseline (the oracle on a bounded sample) + force error ------
     nthreads = os.cpu_count() or 1
@@ -404,6 +420,7 @@ def run_ours(args):
                        fp64_plain_path={"value": fp64_value, "unit": "atom-steps/s", "steps": k64,
                                         "threads_per_atom": fp64_tpa},
                        mixed_over_fp64=value / fp64_value,
+                       macro_err_vs_fp64=macro_err,
                        force_err_vs_fp64_oracle={"mixed": err_mixed, "fp64_plain": err_fp64,
                                                  "atoms_sampled": rows,
                                                  "state": "end of the timed run (thermalised)"},
