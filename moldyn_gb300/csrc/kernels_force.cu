@@ -26,7 +26,9 @@
 // sums are combined by a fixed shuffle tree.  The fused passes of an NVE chunk
 // (NOE) neither sum the per-atom potential and virial nor store them or the
 // forces (both kicks take the forces from registers): the chunk's last,
-// unfused pass writes all three, and nothing reads them in between.
+// unfused pass writes all three, and nothing reads them in between.  The
+// kick/drift FP64 helpers get the FMA-or-not choice as a compile-time
+// constant (a run-time flag made the compiler issue both forms).
 #include "mdgb_internal.cuh"
 
 namespace mdgb {
@@ -534,9 +536,10 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
 // Atoms with a pair whose FP32 r^2 lies within 1e-5 of r_cut^2 (about one in
 // six hundred per step): k_force_mixed leaves them (and their kick/drift) to
 // this kernel, so its hot loop carries no FP64 code and no second pass
-// (measured: ~20 % of the force kernel's time).  One warp per atom, lanes
-// over the list; the band pairs are decided with the reference's FP64
-// arithmetic; every term is rounded to fixed point exactly as in
+// (an inline second pass cost ~9 % of the force kernel's time although it
+// almost never ran).  One warp per atom, lanes over the list; the band pairs
+// are decided with the reference's FP64 arithmetic (no square root: the
+// r^2 threshold of exact_pair); every term is rounded to fixed point exactly as in
 // k_force_mixed (rint(dx * g), here by the conversion instruction), so the
 // force sums are the ones the main kernel would have produced.  Potential and
 // temp are FP32 sums in a fixed shuffle order.
