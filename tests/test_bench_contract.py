@@ -1,0 +1,47 @@
+"""bench.py on the CPU: the reference arm's JSON line (it times the oracle
+port on the host cores, no GPU) and the roofline bookkeeping helpers."""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_the_contract_line():
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--steps", "1", "--warmup", "3"], capture_output=True, text=True, timeout=600,
+                         cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "config", "impl", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["unit"] == "atom-steps/s" and d["value"] > 0
+    assert d["config"]["workload"] == "lj_fcc_1M_nve" and d["config"]["atoms"] == 1_000_000
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["value"] == d["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_fused_fraction_and_roofline_bytes():
+    sys.path.insert(0, ROOT)
+    import bench
+    # a chunk of n NVE steps fuses (n - 1) rounded down to even of its force passes
+    assert bench.fused_fraction(1) == 0.0
+    assert bench.fused_fraction(3) == pytest.approx(2 / 3)
+    assert bench.fused_fraction(64) == pytest.approx(62 / 64)
+    assert bench.fused_fraction(1000) == pytest.approx((15 * 62 + 38) / 1000)
+    # list 4 B x 77.6 candidates + mirror, count, force, potential/temp, velocity
+    assert bench.LIST_CANDIDATES == pytest.approx(77.6, abs=0.05)
+    assert bench.BYTES_PER_ATOM_FORCE == pytest.approx(4 * bench.LIST_CANDIDATES + 108)
+    # a fused pass adds the drift's state traffic and skips force + potential/temp stores
+    assert bench.BYTES_PER_ATOM_DRIFT - bench.BYTES_PER_ATOM_FUSED_SKIP == 60
+    t = bench.ncu_traffic_per_atom()
+    assert t is None or 300.0 < t < 600.0
