@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/mdgb.h"
+#include "host_math.h"
 #include "mdgb_internal.cuh"
 
 namespace mdgb {
@@ -167,17 +168,6 @@ void free_state(mdgb_engine* e) {
 const LJ& pot_of(const mdgb_engine* e, int a, int b) {
     if (a > b) std::swap(a, b);
     return e->pot[a][b].set ? e->pot[a][b] : e->pot_default;
-}
-
-// The smallest double t whose correctly rounded square root exceeds rc: for
-// the reference's test sqrt(r^2) <= rc the same as r^2 < t (sqrt is monotonic
-// and IEEE-exact on the host).
-double sqrt_cut(double rc) {
-    if (!(rc > 0.0) || !std::isfinite(rc)) return rc > 0.0 ? INFINITY : 0.0;
-    double t = rc * rc;
-    while (t > 0.0 && std::sqrt(t) > rc) t = std::nextafter(t, 0.0);
-    while (std::sqrt(t) <= rc) t = std::nextafter(t, INFINITY);
-    return t;
 }
 
 int upload_pairs(mdgb_engine* e) {
