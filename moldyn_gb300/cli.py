@@ -201,30 +201,34 @@ def cmd_solve(args):
     boxes = mio.load_boxes(args.file)
     fps = max(1, args.frames_per_save)
     order = np.argsort(state.ids, kind="stable")
+    ids = state.ids[order]
     done = 0
-    while done < args.iteration_count:
-        if done % fps == 0:
-            out = eng.download()
-            frame = args.state_number + done
-            if len(boxes) > frame:
-                boxes[frame] = out["box"]
-            else:
-                while len(boxes) < frame:
+    # frames are formatted and written on a background thread while the
+    # device runs the next steps
+    with mio.FrameWriter(args.file) as writer:
+        while done < args.iteration_count:
+            if done % fps == 0:
+                out = eng.download()
+                frame = args.state_number + done
+                if len(boxes) > frame:
+                    boxes[frame] = out["box"]
+                else:
+                    while len(boxes) < frame:
+                        boxes.append(out["box"])
                     boxes.append(out["box"])
-                boxes.append(out["box"])
-            mio.save_frame(args.file, frame, state.ids[order], out["pos"][order], out["vel"][order])
-        n = min(fps - done % fps, args.iteration_count - done)
-        eng.step(n, args.delta_time, thermostat=th, target_temperature=t0, barostat=ba, target_pressure=p0)
-        done += n
-    out = eng.download()
-    frame = args.state_number + args.iteration_count
-    while len(boxes) < frame:
-        boxes.append(out["box"])
-    if len(boxes) > frame:
-        boxes[frame] = out["box"]
-    else:
-        boxes.append(out["box"])
-    mio.save_frame(args.file, frame, state.ids[order], out["pos"][order], out["vel"][order])
+                writer.submit(frame, ids, out["pos"][order], out["vel"][order])
+            n = min(fps - done % fps, args.iteration_count - done)
+            eng.step(n, args.delta_time, thermostat=th, target_temperature=t0, barostat=ba, target_pressure=p0)
+            done += n
+        out = eng.download()
+        frame = args.state_number + args.iteration_count
+        while len(boxes) < frame:
+            boxes.append(out["box"])
+        if len(boxes) > frame:
+            boxes[frame] = out["box"]
+        else:
+            boxes.append(out["box"])
+        writer.submit(frame, ids, out["pos"][order], out["vel"][order])
     mio.save_boxes(args.file, boxes)
     eng.close()
 

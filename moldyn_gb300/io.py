@@ -19,6 +19,8 @@ from __future__ import annotations
 
 import csv
 import os
+import queue
+import threading
 
 import numpy as np
 
@@ -62,6 +64,63 @@ def save_frame(directory, frame: int, ids, positions, velocities):
                      f"{fmt_float(v[0])},{fmt_float(v[1])},{fmt_float(v[2])}")
     with open(os.path.join(d, f"{frame}.csv"), "w", newline="") as f:
         f.write("\n".join(lines) + "\n")
+
+
+class FrameWriter:
+    """save_frame on a background thread, so formatting a frame's CSV overlaps
+    the device's next steps (the engine's calls release the interpreter lock
+    while the GPU works).  Frames are written in submission order; at most
+    `depth` wait in the queue (submit blocks beyond that).  A write error is
+    raised by the next submit or by close."""
+
+    def __init__(self, directory, depth: int = 2):
+        self.directory = directory
+        self._q: queue.Queue = queue.Queue(maxsize=max(1, depth))
+        self._error: BaseException | None = None
+        self._thread = threading.Thread(target=self._run, name="frame-writer", daemon=True)
+        self._thread.start()
+
+    def _run(self):
+        while True:
+            item = self._q.get()
+            try:
+                if item is None:
+                    return
+                if self._error is None:
+                    save_frame(self.directory, *item)
+            except BaseException as exc:  # reported on the caller's thread
+                self._error = exc
+            finally:
+                self._q.task_done()
+
+    def _raise(self):
+        if self._error is not None:
+            err, self._error = self._error, None
+            raise err
+
+    def submit(self, frame: int, ids, positions, velocities):
+        """Queue data/<frame>.csv; the arrays must not be modified afterwards."""
+        self._raise()
+        if not self._thread.is_alive():
+            raise RuntimeError("frame writer is closed")
+        self._q.put((frame, ids, positions, velocities))
+
+    def close(self):
+        """Write every queued frame, stop the thread, raise a pending error."""
+        if self._thread.is_alive():
+            self._q.put(None)
+            self._thread.join()
+        self._raise()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        if exc_type is None:
+            self.close()
+        elif self._thread.is_alive():
+            self._q.put(None)
+            self._thread.join()
 
 
 def save_state(directory, frame: int, state: State):

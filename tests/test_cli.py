@@ -135,3 +135,86 @@ def test_cli_solve_with_coupling_and_macro(tmp_path, oracle):
                 "temperature": (2.0 * th) / (3.0 * st.n * K_B) * 100.0}
         for k, v in want.items():
             assert rows[f][k] == v, (f, k, rows[f][k], v)
+
+
+def test_frame_writer_matches_save_frame(tmp_path):
+    """FrameWriter (background thread) writes the same bytes as save_frame,
+    every submitted frame, in order."""
+    from moldyn_gb300 import io as mio
+    rng = np.random.default_rng(8)
+    a, b = str(tmp_path / "a"), str(tmp_path / "b")
+    frames = [(k, rng.integers(0, 3, 50), rng.standard_normal((50, 3)), rng.standard_normal((50, 3)))
+              for k in range(5)]
+    with mio.FrameWriter(a, depth=1) as w:
+        for f in frames:
+            w.submit(*f)
+    for f in frames:
+        mio.save_frame(b, *f)
+    for k in range(5):
+        with open(os.path.join(a, "data", f"{k}.csv"), "rb") as fa, \
+                open(os.path.join(b, "data", f"{k}.csv"), "rb") as fb:
+            assert fa.read() == fb.read()
+
+
+def test_frame_writer_reports_write_errors(tmp_path):
+    from moldyn_gb300 import io as mio
+    blocker = tmp_path / "data"
+    blocker.write_text("a file where the data directory should be")
+    w = mio.FrameWriter(str(tmp_path))
+    w.submit(0, np.zeros(2, dtype=int), np.zeros((2, 3)), np.zeros((2, 3)))
+    with pytest.raises(OSError):
+        w.close()
+
+
+class _FakeEngine:
+    """Stands in for the device engine: moves every atom by (step count) x dt
+    along x, so each saved frame is predictable."""
+
+    def __init__(self):
+        self.steps = 0
+
+    def set_potential_raw(self, *a):
+        pass
+
+    def upload(self, ids, pos, vel, masses, box):
+        self.pos, self.vel, self.box = np.array(pos), np.array(vel), np.array(box, dtype=float)
+
+    def compute_forces(self):
+        pass
+
+    def step(self, n, dt, **kw):
+        self.steps += n
+        self.pos[:, 0] += n * dt
+
+    def download(self):
+        return {"pos": self.pos.copy(), "vel": self.vel.copy(), "force": np.zeros_like(self.pos),
+                "potential": np.zeros(len(self.pos)), "temp": np.zeros(len(self.pos)), "box": self.box.copy()}
+
+    def close(self):
+        pass
+
+
+@pytest.mark.parametrize("fps", [1, 3])
+def test_solve_loop_saves_every_frame(tmp_path, monkeypatch, fps):
+    """commands.rs:258-367 bookkeeping with --frames-per-save, through the
+    background frame writer (device engine replaced by a stand-in)."""
+    from moldyn_gb300 import cli
+    from moldyn_gb300 import io as mio
+    from moldyn_gb300.core import ParticleDatabase, State
+    d = str(tmp_path)
+    ParticleDatabase.clear_particles()
+    ParticleDatabase.add(0, "Argon", 66.335, 0.071)
+    _, pos, vel, _, box = rc.two_argon_moving()
+    mio.save_state(d, 0, State(pos, vel, [0, 0], box))
+    ParticleDatabase.save_particles_data(d)
+    fake = _FakeEngine()
+    monkeypatch.setattr(cli, "_make_engine", lambda args: fake)
+    _cli("-f", d, "--frames-per-save", str(fps), "solve", "-s", "0", "-i", "verlet-method", "-c", "7",
+         "-t", "0.5")
+    assert fake.steps == 7
+    want = [0] + [k for k in range(1, 7) if k % fps == 0] + [7]
+    assert sorted(mio.frame_numbers(d)) == want
+    for k in want:
+        st = mio.load_state(d, k)
+        assert np.allclose(st.positions[:, 0], pos[:, 0] + 0.5 * k)
+    assert len(mio.load_boxes(d)) == 8
