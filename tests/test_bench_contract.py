@@ -45,3 +45,23 @@ def test_fused_fraction_and_roofline_bytes():
     assert bench.BYTES_PER_ATOM_DRIFT - bench.BYTES_PER_ATOM_FUSED_SKIP == 60
     t = bench.ncu_traffic_per_atom()
     assert t is None or 300.0 < t < 600.0
+
+
+def test_headline_system_is_the_documented_workload():
+    """1,000,000 atoms on FCC 50 x 50 x 100 cells at rho* 0.8442 (a = (4/rho*)^(1/3)),
+    inside the box, seeded Maxwell-Boltzmann velocities with zero momentum at T* 0.72."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    pos, vel, box = bench.make_system(seed=1234)
+    a = (4.0 / 0.8442) ** (1.0 / 3.0)
+    assert pos.shape == (1_000_000, 3) and vel.shape == (1_000_000, 3)
+    assert np.allclose(box, np.array([50, 50, 100]) * a)
+    assert (pos >= 0).all() and (pos < box).all()
+    assert len(pos) / np.prod(box) == pytest.approx(0.8442, rel=1e-12)
+    assert np.abs(vel.sum(axis=0)).max() < 1e-6
+    # reduced temperature from the kinetic energy (m = 1, 3N - 3 degrees of freedom ~ 3N)
+    t_star = (vel ** 2).sum() / (3 * len(vel))
+    assert t_star == pytest.approx(0.72, rel=0.01)
+    pos2, vel2, _ = bench.make_system(seed=1234)
+    assert np.array_equal(pos, pos2) and np.array_equal(vel, vel2)
