@@ -68,6 +68,9 @@ def fused_fraction(steps: int, chunk: int = ENGINE_CHUNK) -> float:
     return fused / max(steps, 1)
 
 
+DATA = "synthetic: seeded FCC lattice, rho*=0.8442, Maxwell-Boltzmann T*=0.72, zero momentum"
+
+
 def workload_config(n_atoms):
     name = "lj_fcc_1M_nve" if tuple(CELLS) == (50, 50, 100) else f"lj_fcc_{n_atoms}_nve"
     return {"workload": name, "atoms": int(n_atoms),
@@ -84,6 +87,25 @@ def make_system(seed: int):
     box = np.array(CELLS, dtype=np.float64) * a
     vel = maxwell_boltzmann(len(pos), T_STAR * 100.0 / K_B, 1.0, seed)
     return pos, vel, box
+
+
+def make_positions_oracle():
+    """The same FCC sites as make_system, from the oracle's restatement of
+    initialize_particles_position (the reference arm loads no product code;
+    update_force reads positions only)."""
+    from oracle import oracle as o
+    a = (4.0 / RHO) ** (1.0 / 3.0)
+    pos = o.lattice("FCC", *CELLS, a)
+    box = np.array(CELLS, dtype=np.float64) * a
+    return pos, box
+
+
+def timing_note(st, steps):
+    """How the timed steps ran, from the engine's own counters."""
+    if st.graph_launches:
+        return (f"{st.graph_launches} CUDA-graph replays covering {steps} steps "
+                f"({st.kernel_launches} kernel launches), graphs captured before the timed region")
+    return f"eager launches ({st.kernel_launches} kernel launches)"
 
 
 def dist_info():
@@ -196,34 +218,43 @@ def force_errors(f_gpu, f_ref):
 
 
 def run_reference(args):
+    """The reference algorithm (the oracle's restatement of update_force: an
+    O(N^2) all-pairs FP64 loop, parallel over rows like the reference's
+    rayon loop) on all host threads.  One bench step is one sampled step: a
+    contiguous range of rows of the full all-pairs step, sized so the whole
+    run takes about a minute; the throughput is rows computed per second."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    nthreads = os.cpu_count() or 1
-    pos, vel, box = make_system(seed=1234)
-    n = len(pos)
     from oracle import oracle as o
-    st = o.OracleState([n], pos, vel, [1.0], box, o.pot_table(1, default=(1.0, 1.0)))
-    # size one sampled step so the whole run ends within ~2 minutes
-    per_step = min(0.5, 100.0 / max(args.steps + args.warmup, 1))
-    rows, dt, _, _ = oracle_rows_sample(pos, box, per_step, nthreads)
+    nthreads = os.cpu_count() or 1
+    pos, box = make_positions_oracle()
+    n = len(pos)
+    st = o.OracleState([n], pos, np.zeros_like(pos), [1.0], box, o.pot_table(1, default=(1.0, 1.0)))
+    per_step = min(1.0, max(0.05, 60.0 / max(args.steps + args.warmup, 1)))
+    probe = 16 * nthreads
+    t0 = time.perf_counter()
+    st.update_force(nthreads=nthreads, rows=(0, probe))
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    rows = int(min(n, max(probe, rate * per_step)))
     for _ in range(args.warmup):
         st.update_force(nthreads=nthreads, rows=(0, rows))
     t0 = time.perf_counter()
     for _ in range(args.steps):
         st.update_force(nthreads=nthreads, rows=(0, rows))
     t = time.perf_counter() - t0
-    # one O(N^2) step over all N atoms costs (t/steps) * N/rows; atom-steps/s = rows / (t/steps)
     value = rows * args.steps / t
+    ms_step = 1e3 * t / args.steps
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps * n / rows,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic: seeded FCC lattice, rho*=0.8442, Maxwell-Boltzmann T*=0.72",
-            "impl": "reference",
-            "config": dict(workload_config(n), precision="fp64 (reference algorithm: all-pairs O(N^2))"),
+            "data": DATA, "impl": "reference", "config": workload_config(n),
+            "sampled_step": {"rows": rows, "of_rows": n, "ms": ms_step,
+                             "full_step_ms_extrapolated": ms_step * n / rows,
+                             "note": "a bench step of this arm is rows 0..rows of the all-pairs update_force"},
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": nthreads, "kind": "port",
-                             "sample": f"rows 0..{rows} of one all-pairs update_force per step "
-                                       f"(extrapolated from {rows} of {n} rows)"},
+                             "sample": f"rows 0..{rows} of the {n}-atom all-pairs update_force per step "
+                                       f"(oracle restatement, {nthreads} threads)"},
             "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -265,6 +296,7 @@ def run_ours(args):
         eng.upload(types, pos, vel, [1.0], box)
         eng.compute_forces()
         eng.step(args.warmup, DT)
+        eng.prepare_step(args.steps, DT)     # graph capture (runs nothing) before the timed region
         eng.synchronize()
         eng.reset_stats()
         stream = torch.cuda.ExternalStream(eng.stream_ptr)
@@ -314,43 +346,55 @@ def run_ours(args):
         return
 
     # ---- end to end through the C ABI with host buffers -------------------
+    # upload (host arrays -> device) + initial forces + K steps + download of
+    # the whole state into host arrays, wall clock.  Warm-up: the same calls
+    # once (the second upload of an unchanged shape keeps the device
+    # allocations and the captured graphs, as a user's loop would).
     eng = Engine(precision="mixed", skin=SKIN, threads_per_atom=st.threads_per_atom, device=local,
                  graph_steps=max(args.graph_steps, 0))
     eng.set_potential(0, 0, 1.0, 1.0)
-    eng.upload(types, pos, vel, [1.0], box)       # warm the allocation path
+    host_out = {}
+    eng.upload(types, pos, vel, [1.0], box)
     eng.compute_forces()
     eng.step(args.warmup, DT)
+    eng.prepare_step(args.steps, DT)
+    eng.download(host_out)
     eng.synchronize()
+    eng.reset_stats()
     barrier()
     t0 = time.perf_counter()
     eng.upload(types, pos, vel, [1.0], box)
     eng.compute_forces()
     eng.step(args.steps, DT)
-    out = eng.download()
+    out = eng.download(host_out)
     t_e2e = max_over_ranks(time.perf_counter() - t0)
-    e2e_launches = eng.stats().kernel_launches
+    st_e2e = eng.stats()
     # the reference's solve loop with --frames-per-save 1: one step, then the
     # whole state back to the host, every step
     kf = max(3, min(args.steps, 50))
+    eng.prepare_step(1, DT)
     eng.synchronize()
     barrier()
     t0 = time.perf_counter()
     for _ in range(kf):
         eng.step(1, DT)
-        eng.download()
+        eng.download(host_out)
     t_frames = max_over_ranks(time.perf_counter() - t0)
     eng.close()
-    h2d = n * (3 * 8 + 3 * 8 + 2 + 2 * 4)       # positions, velocities, types, (type, rank) staging
+    h2d = n * (3 * 8 + 3 * 8 + 2)               # positions, velocities, type ids
     d2h = n * (3 * 8 * 3 + 8 + 8)               # positions, velocities, forces, potential, temp
     e2e = {"value": world * n * args.steps / t_e2e, "unit": "atom-steps/s",
            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-           "includes": "upload + initial forces + K steps + download, wall clock",
+           "includes": ("upload of host arrays + initial forces + K steps + download of the whole state "
+                        "into host arrays, wall clock; the copies go straight between the caller's "
+                        "(pageable) arrays and device memory"),
+           "graph_launches": st_e2e.graph_launches, "kernel_launches": st_e2e.kernel_launches,
            "every_step_download": {"value": world * n * kf / t_frames, "unit": "atom-steps/s", "steps": kf,
                                    "d2h_bytes_per_step": d2h,
                                    "includes": "per step: one step, then the full state to host buffers"}}
 
     # ---- plain FP64 GPU path ---------------------------------------------
-    k64 = max(3, min(args.steps, args.fp64_steps))
+    k64 = max(3, min(args.steps, args.fp64_steps or 50))
     eng = Engine(precision="fp64", skin=SKIN, device=local)
     eng.set_potential(0, 0, 1.0, 1.0)
     eng.upload(types, end["pos"], end["vel"], [1.0], box)
@@ -408,11 +452,11 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 pair maths / i64 fixed-point force sums / f64 drift+reductions",
-        "data": "synthetic: seeded FCC lattice, rho*=0.8442, Maxwell-Boltzmann T*=0.72, zero momentum",
-        "config": dict(workload_config(n), precision="mixed", threads_per_atom=st.threads_per_atom,
+        "data": DATA,
+        "config": workload_config(n),
+        "details": dict(precision="mixed", threads_per_atom=st.threads_per_atom,
                        neighbor_capacity=st.neighbor_capacity, rebuilds_in_timed_region=st_g.rebuilds,
-                       timing=(f"chunks of {args.graph_steps} steps replayed as CUDA graphs" if args.graph_steps > 1
-                               else "eager launches"),
+                       timing=timing_note(st_g, args.steps),
                        eager_profiled={"value": world * n * args.steps / (t_prof * 1e-3),
                                        "ms_per_step": t_prof / args.steps,
                                        "note": "per-launch CUDA events; gives the force-kernel time of the roofline"},
@@ -623,7 +667,7 @@ def run_ensemble(args):
         ths = [Thermostat.Berendsen(0.5) for _ in range(nrep)]
         bas = [Barostat.Berendsen(1.0, 5.0) for _ in range(nrep)]
         e.ensemble_set_coupling(ths, t0s, bas, p0)
-        steps = args.steps if prec == "mixed" else max(50, min(args.steps, args.fp64_steps))
+        steps = args.steps if prec == "mixed" else max(50, min(args.steps, args.fp64_steps or 50))
         e.ensemble_step(50, DT)            # warm-up, graph capture
         e.reset_stats()
         if dist is not None:
@@ -706,7 +750,8 @@ def run_drift(args):
     n = len(pos)
     out = {}
     for prec in ("fp32_naive", "mixed", "fp64"):
-        steps = args.steps if prec != "fp64" else min(args.steps, args.fp64_steps)
+        # every variant runs the same steps unless --fp64-steps shortens the FP64 one
+        steps = args.steps if prec != "fp64" or not args.fp64_steps else min(args.steps, args.fp64_steps)
         every = max(1, steps // 100)
         e = Engine(precision=prec, skin=SKIN)
         e.set_potential(0, 0, 1.0, 1.0)
@@ -746,7 +791,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--fp64-steps", type=int, default=50)
+    ap.add_argument("--fp64-steps", type=int, default=None,
+                    help="steps of the plain FP64 leg (default: 50 for lj1m and ensemble; drift: all steps)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cells", default=None,
                     help="FCC unit cells (default 50,50,100 for lj1m, 100,100,200 for lj8m; profiling uses smaller boxes)")

@@ -189,6 +189,13 @@ MDGB_API int mdgb_upload_forces(mdgb_engine* e, const double* force, const doubl
 MDGB_API int mdgb_compute_forces(mdgb_engine* e);
 MDGB_API int mdgb_step(mdgb_engine* e, int64_t nsteps, double dt, mdgb_thermostat* thermostat,
                        mdgb_barostat* barostat);
+/* Capture, without taking a step, the CUDA graphs a later mdgb_step(nsteps,
+ * dt, ...) with these coupling kinds replays (engines with graph_steps > 1;
+ * otherwise a no-op), so the capture is not paid inside that call.  The
+ * coupling structs are only read for their kind.  Graphs stay valid across
+ * uploads of the same shape. */
+MDGB_API int mdgb_prepare_step(mdgb_engine* e, int64_t nsteps, double dt, const mdgb_thermostat* thermostat,
+                               const mdgb_barostat* barostat);
 MDGB_API int mdgb_download_state(mdgb_engine* e, double* pos, double* vel, double* force,
                                  double* potential, double* temp, double box[3]);
 MDGB_API int mdgb_macro_parameters(mdgb_engine* e, int type, mdgb_macro* out);
@@ -203,6 +210,8 @@ MDGB_API int mdgb_ensemble_upload(mdgb_engine* e, int nrep, const int64_t* offse
 MDGB_API int mdgb_ensemble_set_coupling(mdgb_engine* e, const mdgb_thermostat* thermostats,
                                         const mdgb_barostat* barostats);
 MDGB_API int mdgb_ensemble_step(mdgb_engine* e, int64_t nsteps, double dt);
+/* mdgb_prepare_step for ensembles, with the coupling set by mdgb_ensemble_set_coupling. */
+MDGB_API int mdgb_ensemble_prepare(mdgb_engine* e, int64_t nsteps, double dt);
 MDGB_API int mdgb_ensemble_get_coupling(mdgb_engine* e, mdgb_thermostat* thermostats,
                                         mdgb_barostat* barostats);
 MDGB_API int mdgb_ensemble_download(mdgb_engine* e, double* pos, double* vel, double* force,
@@ -226,6 +235,13 @@ MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out);
  * Writes min(n, 14) values. */
 MDGB_API int mdgb_trace_phases(mdgb_engine* e, double* out, int n);
 MDGB_API int mdgb_reset_stats(mdgb_engine* e);
+/* Failure test of the step kernel's bounded grid barrier (no GPU fault): the
+ * next step call's first chunk runs with block hold_block of the step kernel
+ * entering its first barrier after 2 * wait_cycles clock cycles and every
+ * barrier waiting at most wait_cycles.  The other blocks give up, the call
+ * returns MDGB_ERR_DEVICE_TIMEOUT and the state is restored to where the
+ * chunk began, so the engine stays usable. */
+MDGB_API int mdgb_test_barrier_timeout(mdgb_engine* e, int hold_block, int64_t wait_cycles);
 MDGB_API int mdgb_synchronize(mdgb_engine* e);
 
 /* ---- allocation-free force evaluation -------------------------------- */
@@ -233,19 +249,27 @@ MDGB_API int mdgb_synchronize(mdgb_engine* e);
  * memory themselves (a plugin whose host owns all device memory, a loop where
  * an allocation's implicit synchronisation is not allowed, a fixed memory
  * budget): Lennard-Jones forces, potential and temp for n atoms of one type,
- * with the reference's FP64 arithmetic (update_force), using no memory beyond
- * the caller's buffers and one static device array of about 0.9 MB that every
- * GPU loading the library holds until exit.
- *   d_pos      device, 3*n doubles, positions inside [0, box)
- *   box        host, 3 doubles
+ * using no memory beyond the caller's buffers and one static device array of
+ * about 1.2 MB that every GPU loading the library holds until exit.  Each
+ * pair is evaluated with the reference's FP64 arithmetic (update_force), but
+ * the sums run cell by cell rather than in the reference's ascending-j order:
+ * results are deterministic and agree with the reference to about 1e-12 of
+ * the force scale, not bit for bit.
+ *   d_pos      device, 3*n doubles, positions inside [0, box) (others are taken
+ *              to their periodic image for binning)
+ *   box        host, 3 positive finite doubles
  *   d_force    device, 3*n doubles (out); d_potential, d_temp device, n (out, nullable)
  *   stream     cudaStream_t (NULL: the default stream); the call only enqueues work
  * Limits: n <= MDGB_NOALLOC_MAX_ATOMS (else MDGB_ERR_NOALLOC_TOO_LARGE); at most
- * MDGB_NOALLOC_MAX_CELLS cells (larger boxes use coarser cells).  The first call
- * on a device looks up the static array's device address: make it before any
- * stream capture.  Calls share the array: calls that overlap on the GPU race. */
+ * MDGB_NOALLOC_MAX_CELLS cells (larger boxes use coarser cells); an axis
+ * shorter than three cut-off radii is one cell wide, and a box that is one
+ * cell on every axis takes at most MDGB_NOALLOC_MAX_SMALL_BOX atoms.  The
+ * first call on a device looks up the static array's device address: make it
+ * before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU race.  The status covers this call's own launches only. */
 #define MDGB_NOALLOC_MAX_ATOMS 65536
 #define MDGB_NOALLOC_MAX_CELLS 32768
+#define MDGB_NOALLOC_MAX_SMALL_BOX 4096
 MDGB_API int mdgb_forces_noalloc(int64_t n, const double* d_pos, const double box[3], double sigma, double eps,
                                  double* d_force, double* d_potential, double* d_temp, void* stream);
 

@@ -105,6 +105,9 @@ SIGNATURES = {
     "mdgb_compute_forces": (C.c_int, [_E]),
     "mdgb_step": (C.c_int, [_E, C.c_int64, C.c_double, C.POINTER(CThermostat),
                             C.POINTER(CBarostat)]),
+    "mdgb_prepare_step": (C.c_int, [_E, C.c_int64, C.c_double, C.POINTER(CThermostat), C.POINTER(CBarostat)]),
+    "mdgb_ensemble_prepare": (C.c_int, [_E, C.c_int64, C.c_double]),
+    "mdgb_test_barrier_timeout": (C.c_int, [_E, C.c_int, C.c_int64]),
     "mdgb_download_state": (C.c_int, [_E, _opt_dp, _opt_dp, _opt_dp, _opt_dp, _opt_dp, _opt_dp]),
     "mdgb_macro_parameters": (C.c_int, [_E, C.c_int, C.POINTER(CMacro)]),
     "mdgb_ensemble_upload": (C.c_int, [_E, C.c_int, _i64p, _u16p, _dp, _opt_dp, _dp, C.c_int, _dp]),

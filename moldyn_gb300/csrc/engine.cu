@@ -34,7 +34,7 @@ __global__ void k_macro(Dev d, StepParams sp, int sel);
 __global__ void k_apply_pending(Dev d);
 __global__ void k_apply_pending_box(Dev d);
 __global__ void k_gather_out(Dev d, double*, double*, double*, double*, double*);
-__global__ void k_scatter_in(Dev d, const double*, const double*, const int*, const int*);
+__global__ void k_scatter_in(Dev d, const double*, const double*, const uint16_t*, const int*, int);
 __global__ void k_scatter_forces(Dev d, const double*, const double*, const double*);
 __global__ void k_pairs(Dev d, long long capacity, int* out_i, int* out_j, unsigned long long* count);
 using force_fn = void (*)(Dev, StepParams);
@@ -103,10 +103,12 @@ struct mdgb_engine {
     int* snap_i = nullptr;      // [4][N]: orig, rank, cell, slot_of_rank
     float4* snap_mir0 = nullptr;
     RepDev* snap_rep = nullptr;
-    // staging
-    double* d_out = nullptr;     // [11][N] gather-out staging
-    double* h_pin = nullptr;     // pinned host staging [11][N]
-    int* d_in_i = nullptr;       // [2][N] type, rank
+    // device staging in the caller's order; host arrays are copied to and
+    // from it directly (no pinned host copy: on this platform the copy engine
+    // reads and writes pageable memory at full link speed)
+    double* d_out = nullptr;     // [11][N] caller-order staging (pos, vel, force, potential, temp)
+    int* d_in_i = nullptr;       // [N] reference ranks (several types)
+    uint16_t* d_in_t = nullptr;  // [N] caller type ids
     int* h_err = nullptr;        // pinned
     unsigned long long* trace_buf = nullptr;  // per-phase ns of k_pre (MDGB_FLAG_TRACE)
     int lb_grid = 1, lb_cap = -1, lb_ncells = -1;  // list-build launch shape for (cap, cells)
@@ -116,12 +118,34 @@ struct mdgb_engine {
     // coupling (host view of the per-replica settings)
     bool thermo_on = false, baro_on = false, thermo_nh = false;
 
-    // graphs
-    cudaGraphExec_t graph = nullptr;
-    int graph_len = 0;
-    StepParams graph_sp{};
-    bool graph_valid = false;
-    int64_t graph_kernels = 0;   // kernel launches one replay of the graph makes
+    // captured step chunks: one graph per distinct chunk length and launch
+    // parameters (the key holds everything a capture bakes in), replayed
+    // whenever a chunk with the same key comes again; a few are kept
+    struct GraphKey {
+        int len, lb_grid;
+        unsigned flags;
+        int precision;
+        StepParams sp;
+        Dev dev;
+        const void* pos_alt;
+        const void* mir_alt;
+        int class_tpa[3], class_ntiles[3], class_tile_off[3], pad;
+    };
+    struct GraphEntry {
+        GraphKey key;
+        cudaGraphExec_t exec;
+        int64_t kernels;         // kernel launches one replay makes
+        uint64_t used;
+    };
+    std::vector<GraphEntry> graphs;
+    uint64_t graph_clock = 0;
+    // the cells and lists were built at the current positions and nothing has
+    // moved since (a force evaluation can skip its rebuild)
+    bool lists_fresh = false;
+    // failure test of the bounded grid barrier (mdgb_test_barrier_timeout):
+    // the next step call's first chunk holds this block back (-1: off)
+    int test_hold_block = -1;
+    long long test_barrier_cycles = 0;
 
     // stats
     mdgb_stats st{};
@@ -154,15 +178,21 @@ int dalloc(mdgb_engine* e, T** p, size_t count) {
     return MDGB_OK;
 }
 
+void drop_graphs(mdgb_engine* e) {
+    for (auto& g : e->graphs) cudaGraphExecDestroy(g.exec);
+    e->graphs.clear();
+}
+
+// Device allocations of a state (kept by an upload of the same shape).
 void free_state(mdgb_engine* e) {
-    if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
-    e->graph_valid = false;
+    drop_graphs(e);
     for (void* p : e->allocs) cudaFree(p);
     e->allocs.clear();
     if (e->nbr_alloc) { cudaFree(e->nbr_alloc); e->nbr_alloc = nullptr; }
-    if (e->h_pin) { cudaFreeHost(e->h_pin); e->h_pin = nullptr; }
+    e->dev.nn = nullptr;
     e->has_state = false;
     e->forces_valid = false;
+    e->lists_fresh = false;
 }
 
 const LJ& pot_of(const mdgb_engine* e, int a, int b) {
@@ -170,7 +200,9 @@ const LJ& pot_of(const mdgb_engine* e, int a, int b) {
     return e->pot[a][b].set ? e->pot[a][b] : e->pot_default;
 }
 
-int upload_pairs(mdgb_engine* e) {
+// The pair table of the current potentials and the scalars derived from it
+// (largest cut-off, list radius, fixed-point scale), on the host.
+std::vector<PairDev> pair_table(mdgb_engine* e) {
     std::vector<PairDev> tab(MAX_TYPES * MAX_TYPES);
     double fchar = 0.0;
     e->rcmax = 0.0;
@@ -195,8 +227,6 @@ int upload_pairs(mdgb_engine* e) {
                 fchar = std::max(fchar, std::fabs(24.0 * p.eps / p.sigma));
             }
         }
-    CU(cudaMemcpyAsync((void*)e->dev.pair, tab.data(), tab.size() * sizeof(PairDev),
-                       cudaMemcpyHostToDevice, e->stream));
     // fixed-point scale: a power of two putting the characteristic force near 2^31
     if (!(fchar > 0.0)) fchar = 1.0;
     const int ex = 31 - (int)std::ceil(std::log2(fchar));
@@ -209,6 +239,14 @@ int upload_pairs(mdgb_engine* e) {
     e->dev.rlist = e->rlist;
     e->dev.rcmax = e->rcmax;
     e->dev.skin = e->skin;
+    return tab;
+}
+
+int upload_pairs(mdgb_engine* e) {
+    const std::vector<PairDev> tab = pair_table(e);
+    CU(cudaMemcpyAsync((void*)e->dev.pair, tab.data(), tab.size() * sizeof(PairDev),
+                       cudaMemcpyHostToDevice, e->stream));
+    CU(cudaStreamSynchronize(e->stream));   // the table is a local copy
     return MDGB_OK;
 }
 
@@ -226,7 +264,7 @@ int alloc_nbr(mdgb_engine* e, int cap) {
     e->dev.nbr = reinterpret_cast<uint32_t*>(q);
     e->dev.cap = cap;
     e->cap = cap;
-    e->graph_valid = false;
+    e->lists_fresh = false;
     return MDGB_OK;
 }
 
@@ -357,14 +395,22 @@ int launch_force(mdgb_engine* e, const StepParams& sp_in, bool kick) {
 int apply_class_tpa(mdgb_engine* e) {
     CU(cudaMemcpyAsync(e->rep_host.data(), e->dev.rep, e->nrep * sizeof(RepDev), cudaMemcpyDeviceToHost, e->stream));
     CU(cudaStreamSynchronize(e->stream));
-    for (int r = 0; r < e->nrep; ++r) e->rep_host[r].tpa = e->class_tpa[e->class_of[r]];
+    bool changed = false;
+    for (int r = 0; r < e->nrep; ++r) {
+        const int t = e->class_tpa[e->class_of[r]];
+        changed |= e->rep_host[r].tpa != t;
+        e->rep_host[r].tpa = t;
+    }
+    if (!changed) return MDGB_OK;
     CU(cudaMemcpyAsync(e->dev.rep, e->rep_host.data(), e->nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
-    e->graph_valid = false;
+    e->lists_fresh = false;   // the list layout changed
     return MDGB_OK;
 }
 
 StepParams make_sp(const mdgb_engine* e, double dt, bool drift) {
-    StepParams sp{};
+    StepParams sp;
+    std::memset(&sp, 0, sizeof(sp));   // byte-wise comparable (graph keys)
+    sp.hold_block = -1;
     sp.dt = dt;
     for (int t = 0; t < MAX_TYPES; ++t)
         sp.kick_c[t] = t < (int)e->mass.size() ? dt / (2.0 * e->mass[t]) : 0.0;  // integrator.rs:29-30
@@ -448,16 +494,47 @@ int check_flags(mdgb_engine* e, int flags) {
     if (flags & E_FIXED)
         return fail(e, MDGB_ERR_FIXED_POINT_OVERFLOW,
                     "a pair force left the 64-bit fixed-point range (atoms overlapping?)");
+    if (flags & E_INPUT) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "type id >= ntypes");
     if (flags & (E_BOUNDS | E_CELLS)) return fail(e, MDGB_ERR_CUDA, "internal index check failed");
     return MDGB_OK;
 }
 
-int compute_forces_impl(mdgb_engine* e) {
+// Forced rebuild of cells and lists at the current positions; a list that
+// overflows is grown and built again.
+int rebuild_lists(mdgb_engine* e) {
     for (int attempt = 0; attempt < 8; ++attempt) {
         int rc = clear_err(e);
         if (rc) return rc;
         rc = refresh(e, true);
         if (rc) return rc;
+        int flags = 0;
+        rc = read_err(e, &flags);
+        if (rc) return rc;
+        if (flags & E_NLIST) {
+            rc = grow_list(e);
+            if (rc) return rc;
+            e->st.retries++;
+            continue;
+        }
+        rc = check_flags(e, flags);
+        if (rc) return rc;
+        e->lists_fresh = true;
+        return MDGB_OK;
+    }
+    return fail(e, MDGB_ERR_NEIGHBOR_OVERFLOW, "neighbour list kept overflowing");
+}
+
+// update_force: a rebuild (skipped when the lists were just built at these
+// positions -- a second one would give the same cells and lists), then the
+// force pass.
+int compute_forces_impl(mdgb_engine* e) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        int rc = clear_err(e);
+        if (rc) return rc;
+        if (!e->lists_fresh) {
+            rc = refresh(e, true);
+            if (rc) return rc;
+        }
         StepParams sp = make_sp(e, 0.0, false);
         rc = launch_force(e, sp, false);
         if (rc) return rc;
@@ -470,7 +547,10 @@ int compute_forces_impl(mdgb_engine* e) {
             e->st.retries++;
             continue;
         }
-        return check_flags(e, flags);
+        rc = check_flags(e, flags);
+        if (rc) return rc;
+        e->lists_fresh = true;
+        return MDGB_OK;
     }
     return fail(e, MDGB_ERR_NEIGHBOR_OVERFLOW, "neighbour list kept overflowing");
 }
@@ -496,47 +576,87 @@ int run_chunk_kernels(mdgb_engine* e, const StepParams& sp, int n) {
     return MDGB_OK;
 }
 
-bool same_sp(const StepParams& a, const StepParams& b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
+mdgb_engine::GraphKey graph_key(const mdgb_engine* e, const StepParams& sp, int n) {
+    mdgb_engine::GraphKey k;
+    std::memset(&k, 0, sizeof(k));   // padding included: keys compare as bytes
+    k.len = n;
+    k.lb_grid = e->lb_grid;
+    k.flags = e->cfg.flags;
+    k.precision = e->cfg.precision;
+    k.sp = sp;
+    k.dev = e->dev;
+    k.pos_alt = e->pos_alt;
+    k.mir_alt = e->mir_alt;
+    for (int c = 0; c < mdgb_engine::NCLASS; ++c) {
+        k.class_tpa[c] = e->class_tpa[c];
+        k.class_ntiles[c] = e->class_ntiles[c];
+        k.class_tile_off[c] = e->class_tile_off[c];
+    }
+    return k;
+}
+
+// The graph of a chunk of n steps with these parameters, captured on first
+// use (capture runs nothing).  Returns null when graphs are off or capture is
+// not possible here (the engine then stays eager).
+mdgb_engine::GraphEntry* chunk_graph(mdgb_engine* e, const StepParams& sp, int n, int* rc_out) {
+    *rc_out = MDGB_OK;
+    if (!(e->cfg.graph_steps > 1) || (e->cfg.flags & MDGB_FLAG_PROFILE)) return nullptr;
+    // the list-build grid is part of the key: settle it before the lookup
+    if (e->lb_cap != e->dev.cap || e->lb_ncells != e->dev.ncells) {
+        e->lb_grid = list_build_grid(e->dev, e->num_sms);
+        e->lb_cap = e->dev.cap;
+        e->lb_ncells = e->dev.ncells;
+    }
+    const mdgb_engine::GraphKey key = graph_key(e, sp, n);
+    for (auto& g : e->graphs)
+        if (std::memcmp(&g.key, &key, sizeof(key)) == 0) {
+            g.used = ++e->graph_clock;
+            return &g;
+        }
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) { *rc_out = fail(e, MDGB_ERR_CUDA, cudaGetErrorString(ce)); return nullptr; }
+    const int64_t launches0 = e->st.kernel_launches;
+    // capture runs nothing: the buffer pair must read as before afterwards
+    double4_32a* const pos0 = e->dev.pos; double4_32a* const pos1 = e->pos_alt;
+    float4* const mir0 = e->dev.mir; float4* const mir1 = e->mir_alt;
+    int rc = run_chunk_kernels(e, sp, n);
+    ce = cudaStreamEndCapture(e->stream, &g);
+    e->dev.pos = pos0; e->pos_alt = pos1; e->dev.mir = mir0; e->mir_alt = mir1;
+    const int64_t kernels = e->st.kernel_launches - launches0;
+    e->st.kernel_launches = launches0;
+    cudaGraphExec_t exec = nullptr;
+    if (!rc && ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (rc || ce != cudaSuccess) {
+        cudaGetLastError();
+        e->cfg.graph_steps = 0;  // capture unsupported here: stay eager
+        return nullptr;
+    }
+    if (e->graphs.size() >= 6) {   // drop the least recently used
+        size_t lru = 0;
+        for (size_t i = 1; i < e->graphs.size(); ++i)
+            if (e->graphs[i].used < e->graphs[lru].used) lru = i;
+        cudaGraphExecDestroy(e->graphs[lru].exec);
+        e->graphs.erase(e->graphs.begin() + (long)lru);
+    }
+    e->graphs.push_back(mdgb_engine::GraphEntry{key, exec, kernels, ++e->graph_clock});
+    return &e->graphs.back();
+}
 
 int run_chunk(mdgb_engine* e, const StepParams& sp, int n) {
-    const bool use_graph = e->cfg.graph_steps > 1 && !(e->cfg.flags & MDGB_FLAG_PROFILE) &&
-                           n == e->cfg.graph_steps;
-    if (!use_graph) return run_chunk_kernels(e, sp, n);
-    if (!e->graph_valid || e->graph_len != n || !same_sp(e->graph_sp, sp)) {
-        if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
-        cudaGraph_t g = nullptr;
-        CU(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        const int64_t launches0 = e->st.kernel_launches;
-        // capture runs nothing: the buffer pair must read as before afterwards
-        double4_32a* const pos0 = e->dev.pos; double4_32a* const pos1 = e->pos_alt;
-        float4* const mir0 = e->dev.mir; float4* const mir1 = e->mir_alt;
-        int rc = run_chunk_kernels(e, sp, n);
-        cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
-        e->dev.pos = pos0; e->pos_alt = pos1; e->dev.mir = mir0; e->mir_alt = mir1;
-        e->graph_kernels = e->st.kernel_launches - launches0;
-        e->st.kernel_launches = launches0;
-        if (rc || ce != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            cudaGetLastError();
-            e->cfg.graph_steps = 0;  // capture unsupported here: stay eager
-            return run_chunk_kernels(e, sp, n);
-        }
-        ce = cudaGraphInstantiate(&e->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (ce != cudaSuccess) {
-            cudaGetLastError();
-            e->cfg.graph_steps = 0;
-            return run_chunk_kernels(e, sp, n);
-        }
-        e->graph_valid = true;
-        e->graph_len = n;
-        e->graph_sp = sp;
-    }
-    CU(cudaGraphLaunch(e->graph, e->stream));
+    int rc = MDGB_OK;
+    mdgb_engine::GraphEntry* g = chunk_graph(e, sp, n, &rc);
+    if (rc) return rc;
+    if (!g) return run_chunk_kernels(e, sp, n);
+    CU(cudaGraphLaunch(g->exec, e->stream));
     e->st.graph_launches++;
-    e->st.kernel_launches += e->graph_kernels;
+    e->st.kernel_launches += g->kernels;
     return MDGB_OK;
 }
+
+// Chunk lengths a call of nsteps steps runs: full chunks, then the rest.
+int chunk_steps(const mdgb_engine* e) { return e->cfg.graph_steps > 1 ? e->cfg.graph_steps : 64; }
 
 int autotune_tpa(mdgb_engine* e);
 
@@ -548,7 +668,8 @@ int step_impl(mdgb_engine* e, int64_t nsteps, double dt) {
         if (rc) return rc;
     }
     const StepParams sp = make_sp(e, dt, true);
-    const int chunk = e->cfg.graph_steps > 1 ? e->cfg.graph_steps : 64;
+    const int chunk = chunk_steps(e);
+    if (nsteps > 0) e->lists_fresh = false;
     int64_t done = 0;
     int retries = 0;
     while (done < nsteps) {
@@ -557,11 +678,30 @@ int step_impl(mdgb_engine* e, int64_t nsteps, double dt) {
         if (rc) return rc;
         rc = snapshot(e, false);
         if (rc) return rc;
-        rc = run_chunk(e, sp, n);
+        if (e->test_hold_block >= 0) {
+            // the armed failure test: this chunk eager, its first step kernel
+            // with one block held back and a short wait limit
+            StepParams t = sp;
+            t.hold_block = e->test_hold_block;
+            t.barrier_cycles = e->test_barrier_cycles;
+            e->test_hold_block = -1;
+            rc = run_chunk_kernels(e, t, n);
+        } else {
+            rc = run_chunk(e, sp, n);
+        }
         if (rc) return rc;
         int flags = 0;
         rc = read_err(e, &flags);
         if (rc) return rc;
+        if (flags & E_TIMEOUT) {
+            // a grid barrier gave up: the rest of the chunk did nothing; put
+            // the state back as the chunk found it, so the engine stays usable
+            rc = snapshot(e, true);
+            if (!rc) rc = rebuild_lists(e);
+            if (rc) return rc;
+            return fail(e, MDGB_ERR_DEVICE_TIMEOUT,
+                        "a device-side grid barrier timed out; the state is as before the failed chunk");
+        }
         if (flags & E_NLIST) {
             if (++retries > 8) return fail(e, MDGB_ERR_NEIGHBOR_OVERFLOW, "neighbour list kept overflowing");
             rc = grow_list(e);
@@ -593,6 +733,32 @@ int step_impl(mdgb_engine* e, int64_t nsteps, double dt) {
     return MDGB_OK;
 }
 
+// Capture, without running anything, the graphs a call of nsteps steps with
+// these coupling kinds will replay (the full chunk and the remainder), so the
+// first such call does not pay for the capture.
+int prepare_impl(mdgb_engine* e, int64_t nsteps, double dt, bool thermo_on, bool baro_on, bool thermo_nh) {
+    if (!e->has_state) return fail(e, MDGB_ERR_NO_STATE, "no state uploaded");
+    if (nsteps < 0 || !(dt == dt)) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "bad nsteps or dt");
+    if (!(e->cfg.graph_steps > 1)) return MDGB_OK;   // eager engine: nothing to capture
+    if (!e->tuned) {
+        int rc = autotune_tpa(e);
+        if (rc) return rc;
+    }
+    const bool t0 = e->thermo_on, b0 = e->baro_on, n0 = e->thermo_nh;
+    e->thermo_on = thermo_on; e->baro_on = baro_on; e->thermo_nh = thermo_nh;
+    const StepParams sp = make_sp(e, dt, true);
+    e->thermo_on = t0; e->baro_on = b0; e->thermo_nh = n0;
+    const int chunk = chunk_steps(e);
+    const int64_t lens[2] = {std::min<int64_t>(chunk, nsteps), nsteps > chunk ? nsteps % chunk : 0};
+    for (int64_t len : lens) {
+        if (len <= 0) continue;
+        int rc = MDGB_OK;
+        chunk_graph(e, sp, (int)len, &rc);
+        if (rc) return rc;
+    }
+    return MDGB_OK;
+}
+
 // Threads per atom for each size class: every candidate is timed on every
 // class at once (each class's launch bracketed by its own events), and each
 // class keeps its fastest.
@@ -605,8 +771,9 @@ int autotune_tpa(mdgb_engine* e) {
         e->tpa = t;
         int rc = apply_class_tpa(e);
         if (rc) return rc;
-        return refresh(e, true);
+        return e->lists_fresh ? MDGB_OK : rebuild_lists(e);
     }
+    e->lists_fresh = false;
     // Keep the caller's forces: tuning evaluates forces into scratch.
     const size_t N = e->ntot;
     CU(cudaMemcpyAsync(e->snap_d, e->dev.frc, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
@@ -666,11 +833,16 @@ int autotune_tpa(mdgb_engine* e) {
     CU(cudaMemcpyAsync(e->dev.epot, e->snap_d + 3 * N, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     CU(cudaMemcpyAsync(e->dev.evir, e->snap_d + 4 * N, N * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     rc = apply_class_tpa(e);
-    if (!rc) rc = clear_err(e);
     if (rc) return rc;
-    return refresh(e, true);  // lists in the chosen layouts
+    return rebuild_lists(e);  // lists in the chosen layouts
 }
 
+// Upload of a state (one replica or an ensemble).  An upload whose shape
+// (atoms, replicas, tiles, cells, reduction chunks) equals the previous one
+// keeps the device allocations, the neighbour list (if large enough), the
+// tuned threads per atom and the captured graphs; anything else starts over.
+// The caller's arrays are copied straight to the device (pageable memory is
+// fine) and scattered into the device layout by a kernel.
 int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t* type, const double* pos,
                 const double* vel, const double* mass_per_type, int ntypes, const double* boxes) {
     if (nrep < 1 || !offsets || !type || !pos || !mass_per_type || !boxes)
@@ -683,50 +855,53 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     for (int r = 0; r < nrep; ++r) {
         if (offsets[r + 1] <= offsets[r]) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "empty replica");
         for (int a = 0; a < 3; ++a)
-            if (!(boxes[3 * r + a] > 0.0)) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "box must be positive");
+            if (!(boxes[3 * r + a] > 0.0) || !std::isfinite(boxes[3 * r + a]))
+                return fail(e, MDGB_ERR_INVALID_ARGUMENT, "box must be positive and finite");
     }
     for (int t = 0; t < ntypes; ++t)
         if (!(mass_per_type[t] > 0.0)) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "mass must be positive");
-    free_state(e);
-    e->ntot = (int)n;
-    e->nrep = nrep;
-    e->ntypes = ntypes;
-    e->offsets.assign(offsets, offsets + nrep + 1);
-    e->mass.assign(mass_per_type, mass_per_type + ntypes);
-    const int N = e->ntot;
+    const int N = (int)n;
 
-    // reference ranks (type-major within each replica) and per-replica type offsets
-    std::vector<int> rank(N), itype(N);
-    e->rep_host.assign(nrep, RepDev{});
-    for (int r = 0; r < nrep; ++r) {
-        std::vector<int64_t> cnt(ntypes + 1, 0);
-        for (int64_t i = offsets[r]; i < offsets[r + 1]; ++i) {
-            if (type[i] >= ntypes) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "type id >= ntypes");
-            cnt[type[i] + 1]++;
+    // reference ranks (type-major within each replica) and per-replica type
+    // offsets; with one type the rank is the index itself and the type ids are
+    // checked on the device
+    std::vector<int> rank;
+    std::vector<RepDev> reps(nrep, RepDev{});
+    if (ntypes > 1) {
+        rank.resize(N);
+        for (int r = 0; r < nrep; ++r) {
+            std::vector<int64_t> cnt(ntypes + 1, 0);
+            for (int64_t i = offsets[r]; i < offsets[r + 1]; ++i) {
+                if (type[i] >= ntypes) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "type id >= ntypes");
+                cnt[type[i] + 1]++;
+            }
+            for (int t = 0; t < ntypes; ++t)
+                if (cnt[t + 1] == 0)
+                    return fail(e, MDGB_ERR_INVALID_ARGUMENT,
+                                "every type 0..ntypes-1 needs at least one atom in every replica "
+                                "(the reference indexes particles[type][0])");
+            for (int t = 0; t < ntypes; ++t) cnt[t + 1] += cnt[t];
+            RepDev& R = reps[r];
+            for (int t = 0; t <= ntypes; ++t) R.type_off[t] = (int)cnt[t];
+            for (int t = ntypes + 1; t <= MAX_TYPES; ++t) R.type_off[t] = (int)cnt[ntypes];
+            std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+            for (int64_t i = offsets[r]; i < offsets[r + 1]; ++i) rank[i] = (int)(offsets[r] + fill[type[i]]++);
+            R.last_type_count = (int)(cnt[ntypes] - cnt[ntypes - 1]);
         }
-        for (int t = 0; t < ntypes; ++t)
-            if (cnt[t + 1] == 0)
-                return fail(e, MDGB_ERR_INVALID_ARGUMENT,
-                            "every type 0..ntypes-1 needs at least one atom in every replica "
-                            "(the reference indexes particles[type][0])");
-        for (int t = 0; t < ntypes; ++t) cnt[t + 1] += cnt[t];
-        RepDev& R = e->rep_host[r];
-        for (int t = 0; t <= ntypes; ++t) R.type_off[t] = (int)cnt[t];
-        for (int t = ntypes + 1; t <= MAX_TYPES; ++t) R.type_off[t] = (int)cnt[ntypes];
-        std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
-        for (int64_t i = offsets[r]; i < offsets[r + 1]; ++i) {
-            rank[i] = (int)(offsets[r] + fill[type[i]]++);
-            itype[i] = type[i];
+    } else {
+        for (int r = 0; r < nrep; ++r) {
+            RepDev& R = reps[r];
+            const int nr = (int)(offsets[r + 1] - offsets[r]);
+            R.type_off[0] = 0;
+            for (int t = 1; t <= MAX_TYPES; ++t) R.type_off[t] = nr;
+            R.last_type_count = nr;
         }
-        R.last_type_count = (int)(cnt[ntypes] - cnt[ntypes - 1]);
     }
 
-    // potentials, list radius
-    int rc = dalloc(e, (PairDev**)&e->dev.pair, MAX_TYPES * MAX_TYPES);
-    if (rc) return rc;
+    // potentials and list radius (host side: the cell capacity depends on it)
+    e->ntypes = ntypes;
     e->dev.ntypes = ntypes;
-    rc = upload_pairs(e);
-    if (rc) return rc;
+    const std::vector<PairDev> pair_tab = pair_table(e);
 
     // tiles and cells
     std::vector<int4> tiles;
@@ -734,7 +909,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     int max_rep_n = 0;
     double max_density = 0.0;
     for (int r = 0; r < nrep; ++r) {
-        RepDev& R = e->rep_host[r];
+        RepDev& R = reps[r];
         const int nr = (int)(offsets[r + 1] - offsets[r]);
         max_rep_n = std::max(max_rep_n, nr);
         R.begin = offsets[r];
@@ -760,51 +935,106 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         R.myu = 0.0;
         R.rebuild = 1;
     }
-    e->ntiles = (int)tiles.size();
-    e->ncells = (int)cell_rep.size();
+    const int ntiles = (int)tiles.size();
+    const int ncells = (int)cell_rep.size();
     // reduction chunks: runs of <= CHUNK_TILES tiles inside one replica
     std::vector<int4> chunks;
     for (int r = 0; r < nrep; ++r) {
-        RepDev& R = e->rep_host[r];
+        RepDev& R = reps[r];
         R.chunk_begin = (int)chunks.size();
         for (int t = 0; t < R.ntiles; t += CHUNK_TILES)
             chunks.push_back(make_int4(r, R.tile_begin + t, std::min(CHUNK_TILES, R.ntiles - t), 0));
         R.nchunks = (int)chunks.size() - R.chunk_begin;
     }
 
+    // size classes by replica atom count; tile_order = class 0 tiles, class 1, class 2,
+    // costliest (densest replica) first inside a class (persistent kernel)
+    constexpr int NC = mdgb_engine::NCLASS;
+    std::vector<int> class_of(nrep, 0);
+    int class_ntiles[NC] = {0, 0, 0}, class_nrep[NC] = {0, 0, 0};
+    for (int r = 0; r < nrep; ++r) {
+        const int nr = reps[r].n;
+        const int c = nr < 2048 ? 0 : (nr < 32768 ? 1 : 2);
+        class_of[r] = c;
+        reps[r].size_class = c;
+        class_nrep[c]++;
+        class_ntiles[c] += reps[r].ntiles;
+    }
+    std::vector<int> order(ntiles);
+    for (int i = 0; i < ntiles; ++i) order[i] = i;
+    std::vector<double> cost(ntiles);
+    for (int i = 0; i < ntiles; ++i) {
+        const RepDev& R = reps[tiles[i].x];
+        const double vol = R.box[0] * R.box[1] * R.box[2];
+        const double dens = R.n / vol;
+        cost[i] = tiles[i].z * std::min((double)R.n, 1.0 + dens * 4.0 / 3.0 * M_PI * std::pow(e->rlist, 3));
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const int ca = class_of[tiles[a].x], cb = class_of[tiles[b].x];
+        if (ca != cb) return ca < cb;
+        return cost[a] > cost[b];
+    });
+
+    // keep the allocations when the shape is unchanged
     Dev& d = e->dev;
-    d.ntot = N; d.ntiles = e->ntiles; d.nrep = nrep; d.ncells = e->ncells;
+    const bool reuse = e->has_state && N == e->ntot && nrep == e->nrep && ntiles == e->ntiles &&
+                       ncells == e->ncells && (int)chunks.size() == d.nchunks;
+    bool same_classes = reuse;
+    for (int c = 0; c < NC; ++c)
+        same_classes = same_classes && class_ntiles[c] == e->class_ntiles[c] && class_nrep[c] == e->class_nrep[c];
+    if (!reuse) free_state(e);
+    e->has_state = false;
+    e->forces_valid = false;
+    e->lists_fresh = false;
+    e->ntot = N;
+    e->nrep = nrep;
+    e->ntiles = ntiles;
+    e->ncells = ncells;
+    e->offsets.assign(offsets, offsets + nrep + 1);
+    e->mass.assign(mass_per_type, mass_per_type + ntypes);
+    e->rep_host = reps;
+    e->class_of = class_of;
+    for (int c = 0; c < NC; ++c) { e->class_ntiles[c] = class_ntiles[c]; e->class_nrep[c] = class_nrep[c]; }
+    e->class_tile_off[0] = 0;
+    for (int c = 1; c < NC; ++c) e->class_tile_off[c] = e->class_tile_off[c - 1] + e->class_ntiles[c - 1];
+
+    d.ntot = N; d.ntiles = ntiles; d.nrep = nrep; d.ncells = ncells;
     d.refmode = (e->cfg.flags & MDGB_FLAG_REFERENCE_ORDER) && e->cfg.precision == MDGB_PRECISION_FP64 ? 1 : 0;
     d.mixed = e->cfg.precision != MDGB_PRECISION_FP64 ? 1 : 0;
     d.single_type = ntypes == 1 ? 1 : 0;
     d.last_type = ntypes - 1;
     for (int t = 0; t < MAX_TYPES; ++t) d.mass[t] = t < ntypes ? mass_per_type[t] : 1.0;
 
-    if ((rc = dalloc(e, &d.pos, N)) || (rc = dalloc(e, &d.vel, 3 * (size_t)N)) ||
-        (rc = dalloc(e, &d.frc, 3 * (size_t)N)) || (rc = dalloc(e, &d.epot, N)) ||
-        (rc = dalloc(e, &d.evir, N)) || (rc = dalloc(e, &d.mir, N)) || (rc = dalloc(e, &d.mir0, N)) ||
-        (rc = dalloc(e, &e->pos_alt, N)) || (rc = dalloc(e, &e->mir_alt, N)) ||
-        (rc = dalloc(e, &d.band_list, N)) || (rc = dalloc(e, &d.band_count, 1)) ||
-        (rc = dalloc(e, &d.cell, N)) || (rc = dalloc(e, &d.orig, N)) || (rc = dalloc(e, &d.rank, N)) ||
-        (rc = dalloc(e, &d.nn, N)) || (rc = dalloc(e, &d.tiles, e->ntiles)) ||
-        (rc = dalloc(e, &d.rep, nrep)) || (rc = dalloc(e, &d.part, 8 * (size_t)e->ntiles)) ||
-        (rc = dalloc(e, &d.cpart, 8 * chunks.size())) || (rc = dalloc(e, &d.chunks, chunks.size())) ||
-        (rc = dalloc(e, &d.err, 2)) || (rc = dalloc(e, &d.max_needed, 1)) ||
-        (rc = dalloc(e, &d.cell_count, e->ncells)) ||
-        (rc = dalloc(e, &d.cell_start, e->ncells + 1)) || (rc = dalloc(e, &d.cell_rep, e->ncells)) ||
-        (rc = dalloc(e, &d.perm, N)) || (rc = dalloc(e, &d.tmp_pos, N)) ||
-        (rc = dalloc(e, &d.tmp_d, 8 * (size_t)N)) || (rc = dalloc(e, &d.tmp_i, 4 * (size_t)N)) ||
-        (rc = dalloc(e, &d.slot_of_rank, N)) || (rc = dalloc(e, &d.bsum, 4096)) ||
-        (rc = dalloc(e, &d.bar, 4)) || (rc = dalloc(e, &d.queue, mdgb_engine::NCLASS)) ||
-        (rc = dalloc(e, &e->trace_buf, TR_SLOTS)) ||
-        (rc = dalloc(e, &d.tile_order, e->ntiles)) ||
-        (rc = dalloc(e, &e->snap_pos, N)) || (rc = dalloc(e, &e->snap_d, 8 * (size_t)N)) ||
-        (rc = dalloc(e, &e->snap_i, 4 * (size_t)N)) || (rc = dalloc(e, &e->snap_mir0, N)) ||
-        (rc = dalloc(e, &e->snap_rep, nrep)) || (rc = dalloc(e, &e->d_out, 11 * (size_t)N)) ||
-        (rc = dalloc(e, &e->d_in_i, 2 * (size_t)N)))
-        return rc;
-    CU(cudaMallocHost((void**)&e->h_pin, 11 * (size_t)N * sizeof(double)));
+    int rc = MDGB_OK;
+    if (!reuse) {
+        if ((rc = dalloc(e, (PairDev**)&d.pair, MAX_TYPES * MAX_TYPES)) ||
+            (rc = dalloc(e, &d.pos, N)) || (rc = dalloc(e, &d.vel, 3 * (size_t)N)) ||
+            (rc = dalloc(e, &d.frc, 3 * (size_t)N)) || (rc = dalloc(e, &d.epot, N)) ||
+            (rc = dalloc(e, &d.evir, N)) || (rc = dalloc(e, &d.mir, N)) || (rc = dalloc(e, &d.mir0, N)) ||
+            (rc = dalloc(e, &e->pos_alt, N)) || (rc = dalloc(e, &e->mir_alt, N)) ||
+            (rc = dalloc(e, &d.band_list, N)) || (rc = dalloc(e, &d.band_count, 1)) ||
+            (rc = dalloc(e, &d.cell, N)) || (rc = dalloc(e, &d.orig, N)) || (rc = dalloc(e, &d.rank, N)) ||
+            (rc = dalloc(e, &d.nn, N)) || (rc = dalloc(e, &d.tiles, ntiles)) ||
+            (rc = dalloc(e, &d.rep, nrep)) || (rc = dalloc(e, &d.part, 8 * (size_t)ntiles)) ||
+            (rc = dalloc(e, &d.cpart, 8 * chunks.size())) || (rc = dalloc(e, &d.chunks, chunks.size())) ||
+            (rc = dalloc(e, &d.err, 2)) || (rc = dalloc(e, &d.max_needed, 1)) ||
+            (rc = dalloc(e, &d.cell_count, ncells)) ||
+            (rc = dalloc(e, &d.cell_start, ncells + 1)) || (rc = dalloc(e, &d.cell_rep, ncells)) ||
+            (rc = dalloc(e, &d.perm, N)) || (rc = dalloc(e, &d.tmp_pos, N)) ||
+            (rc = dalloc(e, &d.tmp_d, 8 * (size_t)N)) || (rc = dalloc(e, &d.tmp_i, 4 * (size_t)N)) ||
+            (rc = dalloc(e, &d.slot_of_rank, N)) || (rc = dalloc(e, &d.bsum, 4096)) ||
+            (rc = dalloc(e, &d.bar, 4)) || (rc = dalloc(e, &d.queue, NC)) ||
+            (rc = dalloc(e, &e->trace_buf, TR_SLOTS)) ||
+            (rc = dalloc(e, &d.tile_order, ntiles)) ||
+            (rc = dalloc(e, &e->snap_pos, N)) || (rc = dalloc(e, &e->snap_d, 8 * (size_t)N)) ||
+            (rc = dalloc(e, &e->snap_i, 4 * (size_t)N)) || (rc = dalloc(e, &e->snap_mir0, N)) ||
+            (rc = dalloc(e, &e->snap_rep, nrep)) || (rc = dalloc(e, &e->d_out, 11 * (size_t)N)) ||
+            (rc = dalloc(e, &e->d_in_i, N)) || (rc = dalloc(e, &e->d_in_t, N)))
+            return rc;
+    }
     if (!e->h_err) CU(cudaMallocHost((void**)&e->h_err, 4 * sizeof(int)));
+    CU(cudaMemcpyAsync((void*)d.pair, pair_tab.data(), pair_tab.size() * sizeof(PairDev), cudaMemcpyHostToDevice,
+                       e->stream));
 
     // neighbour capacity from the densest replica (grows on overflow)
     int cap = e->cfg.neighbor_capacity;
@@ -814,99 +1044,62 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         cap = std::min(cap, std::max(max_rep_n - 1, 8));
     }
     cap = std::max(8, (cap + 7) & ~7);
-    rc = alloc_nbr(e, cap);
-    if (rc) return rc;
+    if (!e->nbr_alloc || cap > e->cap) {
+        rc = alloc_nbr(e, cap);
+        if (rc) return rc;
+    }
     e->st = mdgb_stats{};
-    e->st.neighbor_capacity = cap;
+    e->st.neighbor_capacity = e->cap;
 
-    // tile order for the persistent kernel: costliest (densest replica) first
-    std::vector<int> order(e->ntiles);
-    for (int i = 0; i < e->ntiles; ++i) order[i] = i;
-    std::vector<double> cost(e->ntiles);
-    for (int i = 0; i < e->ntiles; ++i) {
-        const RepDev& R = e->rep_host[tiles[i].x];
-        const double vol = R.box[0] * R.box[1] * R.box[2];
-        const double dens = R.n / vol;
-        cost[i] = tiles[i].z * std::min((double)R.n, 1.0 + dens * 4.0 / 3.0 * M_PI * std::pow(e->rlist, 3));
+    // threads per atom: kept from the last tuning when the size classes are
+    // the same, else the configured (or default) value until the next tuning
+    if (!same_classes) {
+        const int t0 = d.refmode ? 1 : (e->cfg.threads_per_atom > 0 ? e->cfg.threads_per_atom : 1);
+        for (int c = 0; c < NC; ++c) e->class_tpa[c] = t0;
+        e->tuned = false;
     }
-    // size classes by replica atom count; tile_order = class 0 tiles, class 1, class 2
-    e->class_of.assign(nrep, 0);
-    for (int c = 0; c < mdgb_engine::NCLASS; ++c) { e->class_ntiles[c] = 0; e->class_nrep[c] = 0; }
-    for (int r = 0; r < nrep; ++r) {
-        const int nr = e->rep_host[r].n;
-        const int c = nr < 2048 ? 0 : (nr < 32768 ? 1 : 2);
-        e->class_of[r] = c;
-        e->rep_host[r].size_class = c;
-        e->class_nrep[c]++;
-        e->class_ntiles[c] += e->rep_host[r].ntiles;
-    }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        const int ca = e->class_of[tiles[a].x], cb = e->class_of[tiles[b].x];
-        if (ca != cb) return ca < cb;
-        return cost[a] > cost[b];
-    });
-    e->class_tile_off[0] = 0;
-    for (int c = 1; c < mdgb_engine::NCLASS; ++c) e->class_tile_off[c] = e->class_tile_off[c - 1] + e->class_ntiles[c - 1];
+    for (int r = 0; r < nrep; ++r) e->rep_host[r].tpa = e->class_tpa[e->class_of[r]];
+    e->tpa = e->class_tpa[0];
+    for (int c = NC - 1; c >= 0; --c)
+        if (e->class_ntiles[c]) { e->tpa = e->class_tpa[c]; break; }
+    d.tpa = e->tpa;
 
     CU(cudaMemcpyAsync(d.tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, e->stream));
     d.nchunks = (int)chunks.size();
     CU(cudaMemcpyAsync(d.chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice, e->stream));
     CU(cudaMemcpyAsync(d.tile_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream));
     CU(cudaMemcpyAsync(d.cell_rep, cell_rep.data(), cell_rep.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream));
-    CU(cudaMemsetAsync(d.cell_count, 0, e->ncells * sizeof(int), e->stream));
+    CU(cudaMemsetAsync(d.cell_count, 0, ncells * sizeof(int), e->stream));
     CU(cudaMemsetAsync(d.max_needed, 0, sizeof(int), e->stream));
     CU(cudaMemsetAsync(e->trace_buf, 0, TR_SLOTS * sizeof(unsigned long long), e->stream));
     d.trace = (e->cfg.flags & MDGB_FLAG_TRACE) ? e->trace_buf : nullptr;
     CU(cudaMemsetAsync(d.err, 0, 2 * sizeof(int), e->stream));
     CU(cudaMemsetAsync(d.bar, 0, 4 * sizeof(unsigned int), e->stream));
-    {
-        const int t0 = (e->cfg.flags & MDGB_FLAG_REFERENCE_ORDER) && e->cfg.precision == MDGB_PRECISION_FP64
-                           ? 1 : (e->cfg.threads_per_atom > 0 ? e->cfg.threads_per_atom : 1);
-        for (int c = 0; c < mdgb_engine::NCLASS; ++c) e->class_tpa[c] = t0;
-        for (int r = 0; r < nrep; ++r) e->rep_host[r].tpa = t0;
-    }
     CU(cudaMemcpyAsync(d.rep, e->rep_host.data(), nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
-    // staging copies of the caller's arrays
+    // the caller's arrays, straight to the device staging
     double* dpos = e->d_out;
     double* dvel = e->d_out + 3 * (size_t)N;
-    std::memcpy(e->h_pin, pos, 3 * (size_t)N * sizeof(double));
-    if (vel) std::memcpy(e->h_pin + 3 * (size_t)N, vel, 3 * (size_t)N * sizeof(double));
-    CU(cudaMemcpyAsync(dpos, e->h_pin, (vel ? 6 : 3) * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
-    int* hi = reinterpret_cast<int*>(e->h_pin + 6 * (size_t)N);
-    CU(cudaStreamSynchronize(e->stream));
-    std::memcpy(hi, itype.data(), N * sizeof(int));
-    std::memcpy(hi + N, rank.data(), N * sizeof(int));
-    CU(cudaMemcpyAsync(e->d_in_i, hi, 2 * (size_t)N * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+    CU(cudaMemcpyAsync(dpos, pos, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    if (vel) CU(cudaMemcpyAsync(dvel, vel, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    CU(cudaMemcpyAsync(e->d_in_t, type, (size_t)N * sizeof(uint16_t), cudaMemcpyHostToDevice, e->stream));
+    if (ntypes > 1)
+        CU(cudaMemcpyAsync(e->d_in_i, rank.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, e->stream));
     const double* vptr = vel ? dvel : nullptr;
-    const int* tptr = e->d_in_i;
-    const int* rptr = e->d_in_i + N;
-    void* args[] = {(void*)&e->dev, (void*)&dpos, (void*)&vptr, (void*)&tptr, (void*)&rptr};
+    const uint16_t* tptr = e->d_in_t;
+    const int* rptr = ntypes > 1 ? e->d_in_i : nullptr;
+    int nt = ntypes;
+    void* args[] = {(void*)&e->dev, (void*)&dpos, (void*)&vptr, (void*)&tptr, (void*)&rptr, (void*)&nt};
     CU(cudaLaunchKernel((const void*)k_scatter_in, dim3((N + 255) / 256), dim3(256), args, 0, e->stream));
-    CU(cudaStreamSynchronize(e->stream));
-    e->has_state = true;
-    e->forces_valid = false;
     e->thermo_on = e->baro_on = e->thermo_nh = false;
-    e->tuned = false;
-    e->tpa = e->class_tpa[0];
-    d.tpa = e->tpa;
-    // bin and build lists now, so a bare mdgb_step starts from a valid list
-    rc = clear_err(e);
-    if (rc) return rc;
-    rc = refresh(e, true);
-    if (rc) return rc;
-    int flags = 0;
-    rc = read_err(e, &flags);
-    if (rc) return rc;
-    if (flags & E_NLIST) {
-        rc = grow_list(e);
-        if (rc) return rc;
-        rc = clear_err(e);
-        if (!rc) rc = refresh(e, true);
-        if (rc) return rc;
+    if (ntypes == 1) {   // the type ids were checked on the device
+        int flags = 0;
         rc = read_err(e, &flags);
         if (rc) return rc;
+        if (flags) return check_flags(e, flags);
     }
-    return check_flags(e, flags & ~E_NLIST);
+    e->has_state = true;
+    // bin and build lists now, so a bare mdgb_step starts from a valid list
+    return rebuild_lists(e);
 }
 
 int set_coupling_impl(mdgb_engine* e, const mdgb_thermostat* th, const mdgb_barostat* ba) {
@@ -931,10 +1124,6 @@ int set_coupling_impl(mdgb_engine* e, const mdgb_thermostat* th, const mdgb_baro
             R.myu = ba[r].myu;
         }
     }
-    if (any_nh && e->ntypes > 1)
-        return fail(e, MDGB_ERR_UNSUPPORTED,
-                    "Nose-Hoover coupling is implemented for single-type systems (the reference's per-type "
-                    "psi accumulation across several types is not)");
     e->thermo_nh = any_nh;
     e->thermo_on = th != nullptr;
     e->baro_on = ba != nullptr;
@@ -953,22 +1142,32 @@ int get_coupling_impl(mdgb_engine* e, mdgb_thermostat* th, mdgb_barostat* ba) {
     return MDGB_OK;
 }
 
+// The requested arrays gathered into the caller's order on the device, then
+// copied straight into the caller's buffers (pageable memory is fine).
 int download_impl(mdgb_engine* e, double* pos, double* vel, double* force, double* pot, double* temp,
                   double* boxes) {
     if (!e->has_state) return fail(e, MDGB_ERR_NO_STATE, "no state uploaded");
     const size_t N = e->ntot;
     double* o = e->d_out;
-    double *op = o, *ov = o + 3 * N, *of = o + 6 * N, *oe = o + 9 * N, *ot = o + 10 * N;
-    void* args[] = {(void*)&e->dev, (void*)&op, (void*)&ov, (void*)&of, (void*)&oe, (void*)&ot};
-    CU(cudaLaunchKernel((const void*)k_gather_out, dim3((unsigned)((N + 255) / 256)), dim3(256), args, 0, e->stream));
-    CU(cudaMemcpyAsync(e->h_pin, e->d_out, 11 * N * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
-    CU(cudaMemcpyAsync(e->rep_host.data(), e->dev.rep, e->nrep * sizeof(RepDev), cudaMemcpyDeviceToHost, e->stream));
+    double* op = pos ? o : nullptr;
+    double* ov = vel ? o + 3 * N : nullptr;
+    double* of = force ? o + 6 * N : nullptr;
+    double* oe = pot ? o + 9 * N : nullptr;
+    double* ot = temp ? o + 10 * N : nullptr;
+    if (op || ov || of || oe || ot) {
+        void* args[] = {(void*)&e->dev, (void*)&op, (void*)&ov, (void*)&of, (void*)&oe, (void*)&ot};
+        CU(cudaLaunchKernel((const void*)k_gather_out, dim3((unsigned)((N + 255) / 256)), dim3(256), args, 0,
+                            e->stream));
+    }
+    if (pos) CU(cudaMemcpyAsync(pos, op, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    if (vel) CU(cudaMemcpyAsync(vel, ov, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    if (force) CU(cudaMemcpyAsync(force, of, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    if (pot) CU(cudaMemcpyAsync(pot, oe, N * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    if (temp) CU(cudaMemcpyAsync(temp, ot, N * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    if (boxes)
+        CU(cudaMemcpyAsync(e->rep_host.data(), e->dev.rep, e->nrep * sizeof(RepDev), cudaMemcpyDeviceToHost,
+                           e->stream));
     CU(cudaStreamSynchronize(e->stream));
-    if (pos) std::memcpy(pos, e->h_pin, 3 * N * sizeof(double));
-    if (vel) std::memcpy(vel, e->h_pin + 3 * N, 3 * N * sizeof(double));
-    if (force) std::memcpy(force, e->h_pin + 6 * N, 3 * N * sizeof(double));
-    if (pot) std::memcpy(pot, e->h_pin + 9 * N, N * sizeof(double));
-    if (temp) std::memcpy(temp, e->h_pin + 10 * N, N * sizeof(double));
     if (boxes)
         for (int r = 0; r < e->nrep; ++r)
             for (int a = 0; a < 3; ++a) boxes[3 * r + a] = e->rep_host[r].box[a];
@@ -1119,7 +1318,7 @@ static int set_pot(mdgb_engine* e, uint16_t t0, uint16_t t1, const LJ& p) {
         cudaSetDevice(e->device);
         int rc = upload_pairs(e);
         if (rc) return rc;
-        e->graph_valid = false;
+        e->lists_fresh = false;
         // a changed cutoff needs lists built with the new radius
         CU(cudaMemcpyAsync(e->rep_host.data(), e->dev.rep, e->nrep * sizeof(RepDev), cudaMemcpyDeviceToHost,
                            e->stream));
@@ -1172,11 +1371,9 @@ MDGB_API int mdgb_upload_forces(mdgb_engine* e, const double* force, const doubl
     double* d_f = e->d_out;
     double* d_p = e->d_out + 3 * N;
     double* d_t = e->d_out + 4 * N;
-    CU(cudaStreamSynchronize(e->stream));
-    if (force) std::memcpy(e->h_pin, force, 3 * N * sizeof(double));
-    if (potential) std::memcpy(e->h_pin + 3 * N, potential, N * sizeof(double));
-    if (temp) std::memcpy(e->h_pin + 4 * N, temp, N * sizeof(double));
-    CU(cudaMemcpyAsync(e->d_out, e->h_pin, 5 * N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    if (force) CU(cudaMemcpyAsync(d_f, force, 3 * N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    if (potential) CU(cudaMemcpyAsync(d_p, potential, N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    if (temp) CU(cudaMemcpyAsync(d_t, temp, N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
     const double* a = force ? d_f : nullptr;
     const double* b = potential ? d_p : nullptr;
     const double* c = temp ? d_t : nullptr;
@@ -1242,6 +1439,28 @@ MDGB_API int mdgb_step(mdgb_engine* e, int64_t nsteps, double dt, mdgb_thermosta
     rc = step_impl(e, nsteps, dt);
     if (rc) return rc;
     return get_coupling_impl(e, thermostat, barostat);
+}
+
+MDGB_API int mdgb_prepare_step(mdgb_engine* e, int64_t nsteps, double dt, const mdgb_thermostat* thermostat,
+                               const mdgb_barostat* barostat) {
+    if (!e) return MDGB_ERR_INVALID_ARGUMENT;
+    if (e->nrep != 1 && e->has_state) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "ensemble engine: use mdgb_ensemble_prepare");
+    cudaSetDevice(e->device);
+    const bool nh = thermostat && thermostat->kind == MDGB_THERMOSTAT_NOSE_HOOVER;
+    return prepare_impl(e, nsteps, dt, thermostat != nullptr, barostat != nullptr, nh);
+}
+
+MDGB_API int mdgb_ensemble_prepare(mdgb_engine* e, int64_t nsteps, double dt) {
+    if (!e) return MDGB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(e->device);
+    return prepare_impl(e, nsteps, dt, e->thermo_on, e->baro_on, e->thermo_nh);
+}
+
+MDGB_API int mdgb_test_barrier_timeout(mdgb_engine* e, int hold_block, int64_t wait_cycles) {
+    if (!e || hold_block < 0 || wait_cycles <= 0) return MDGB_ERR_INVALID_ARGUMENT;
+    e->test_hold_block = hold_block;
+    e->test_barrier_cycles = wait_cycles;
+    return MDGB_OK;
 }
 
 MDGB_API int mdgb_download_state(mdgb_engine* e, double* pos, double* vel, double* force, double* potential,

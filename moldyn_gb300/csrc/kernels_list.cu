@@ -56,6 +56,7 @@ template <bool SINGLE>
 // slower).
 __global__ void __launch_bounds__(LB_WARPS * 32, 11) k_build_list(Dev d) {
     if (*(volatile const unsigned int*)(d.bar + 2) == 0u) return;   // no rebuild this step
+    if (chunk_failed(d)) return;
     extern __shared__ __align__(16) uint32_t lb_smem[];
     __shared__ int s_last;
     const unsigned FULL = 0xffffffffu;

@@ -69,7 +69,24 @@ __device__ __forceinline__ double4_32a ldcg4(const double4_32a* p) {
     return make_double4_32a(a.x, a.y, b.x, b.y);
 }
 
-__device__ __forceinline__ void grid_barrier(const Dev& d) {
+// The grid barrier's wait limit in clock cycles (set at kernel entry) and the
+// block's verdict after the last barrier.
+__shared__ long long g_bar_limit;
+__shared__ int g_bar_abort;
+
+__device__ __forceinline__ void barrier_setup(const StepParams& sp) {
+    if (threadIdx.x == 0) {
+        g_bar_limit = sp.barrier_cycles > 0 ? sp.barrier_cycles : BARRIER_LIMIT_CYCLES;
+        g_bar_abort = 0;
+    }
+}
+
+// Returns true when the launch must stop: this block's wait ran out, or
+// another block's did (E_TIMEOUT in the error word).  A block that stops
+// does no work of the next phase, so no phase ever reads the incomplete
+// results of the one before; every block ends at its next barrier at the
+// latest, each wait being bounded.  Call sites: if (grid_barrier(d)) return;
+__device__ __forceinline__ bool grid_barrier(const Dev& d) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int* gen = d.bar + 1;
@@ -84,7 +101,7 @@ __device__ __forceinline__ void grid_barrier(const Dev& d) {
             const long long t0 = clock64();
             while (*gen == g) {
                 __nanosleep(100);
-                if (clock64() - t0 > BARRIER_LIMIT_CYCLES) {
+                if (clock64() - t0 > g_bar_limit) {
                     atomicOr(d.err, E_TIMEOUT);
                     break;
                 }
@@ -92,8 +109,10 @@ __device__ __forceinline__ void grid_barrier(const Dev& d) {
         }
         __threadfence();
         g_tile_rep_id = -1;
+        g_bar_abort = (*(volatile int*)d.err & E_TIMEOUT) ? 1 : 0;
     }
     __syncthreads();
+    return g_bar_abort != 0;
 }
 
 // Deterministic block sum of NV doubles (fixed shuffle tree, fixed warp order).
@@ -474,6 +493,28 @@ __device__ void phase_serial(const Dev& d, const StepParams& sp, int sel, bool c
         W->count = e - b; W->T = T; W->P = P;
         if (coupling) coupling_factors(W, R, T, P, sp.dt);
     }
+}
+
+// psi += psi_dot(T_t) * dt/2 with T_t the temperature of the atoms of type t
+// (thermostat.rs:35-39 before the kick, :59-65 after it), per replica with a
+// Nose-Hoover thermostat.  Returns true when the launch must stop.
+__device__ __forceinline__ bool nh_psi_of_type(const Dev& d, const StepParams& sp, int t) {
+    if (d.refmode) {
+        phase_serial(d, sp, t, false, true);
+        return grid_barrier(d);
+    }
+    phase_partials1(d, t);
+    if (grid_barrier(d)) return true;
+    phase_chunk_sums<7>(d);
+    if (grid_barrier(d)) return true;
+    phase_finalize1(d, t);
+    if (grid_barrier(d)) return true;
+    phase_partials2(d, t);
+    if (grid_barrier(d)) return true;
+    phase_chunk_sums<1>(d);
+    if (grid_barrier(d)) return true;
+    phase_finalize_nh(d, sp, t);
+    return grid_barrier(d);
 }
 
 // ---------------------------------------------------------------------------
@@ -974,7 +1015,16 @@ __device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp
 // 6 blocks of 128 threads per SM (80 registers): at the default 64 registers
 // the phases spilled (measured: the rebuild's sort phases ran ~1.8x slower).
 __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
+    if (chunk_failed(d)) return;
+    barrier_setup(sp);
     tile_rep_reset();
+    if (sp.hold_block == (int)blockIdx.x && threadIdx.x == 0) {
+        // failure test: this block enters its first barrier after the others
+        // have given up waiting (a bounded delay of twice the wait limit)
+        const long long t0 = clock64();
+        while (clock64() - t0 < 2 * g_bar_limit) __nanosleep(1000);
+    }
+    __syncthreads();
     PhaseClock clk(d.trace);
     if (sp.predrifted) {
         // the fused force pass of the previous step kicked and drifted (NVE
@@ -997,7 +1047,7 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
             return;
         }
         phase_decide(d, sp);
-        grid_barrier(d);
+        if (grid_barrier(d)) return;
         clk.mark(TR_DECIDE);
         if (*(volatile unsigned int*)(d.bar + 2) == 0u) return;
         if (clk.tr) atomicAdd(clk.tr + TR_REBUILD_LAUNCHES, 1ull);
@@ -1006,61 +1056,56 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
     }
     if (sp.do_drift && sp.coupled) {
         const int sel = d.last_type;
+        // Nose-Hoover with several types: calculate_lambda runs once per type,
+        // each adding its psi_dot * dt/2 (thermostat.rs:35-39, called per type
+        // from integrator.rs:23-26); the last type's pass below adds its own
+        // and sets lambda from the sum
+        if (sp.thermo_nh)
+            for (int t = 0; t < sel; ++t)
+                if (nh_psi_of_type(d, sp, t)) return;
         if (d.refmode) {
             phase_serial(d, sp, sel, true);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
         } else if (d.mixed) {
             phase_partials1(d, sel);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
             phase_chunk_sums<7>(d);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
             phase_finalize_single(d, sp, sel);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
         } else {
             phase_partials1(d, sel);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
             phase_chunk_sums<7>(d);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
             phase_finalize1(d, sel);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
             phase_partials2(d, sel);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
             phase_chunk_sums<1>(d);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
             phase_finalize2(d, sp, true, sel);
-            grid_barrier(d);
+            if (grid_barrier(d)) return;
         }
         clk.mark(TR_COUPLING);
     }
     if (sp.do_drift && sp.thermo_nh) {
-        const int sel = d.last_type;
         if (d.mixed) phase_kick<true>(d, sp); else phase_kick<false>(d, sp);
-        grid_barrier(d);
-        if (d.refmode) {
-            phase_serial(d, sp, sel, false, true);
-            grid_barrier(d);
-        } else {
-            phase_partials1(d, sel);
-            grid_barrier(d);
-            phase_chunk_sums<7>(d);
-            grid_barrier(d);
-            phase_finalize1(d, sel);
-            grid_barrier(d);
-            phase_partials2(d, sel);
-            grid_barrier(d);
-            phase_chunk_sums<1>(d);
-            grid_barrier(d);
-            phase_finalize_nh(d, sp, sel);
-            grid_barrier(d);
-        }
+        if (grid_barrier(d)) return;
+        // Thermostat::update per type after the kick (integrator.rs:35-39):
+        // each type's temperature before its scaling adds psi_dot * dt/2
+        // (thermostat.rs:59-65); the scaling itself uses the lambda computed
+        // before the kick, in the drift phase
+        for (int t = 0; t <= d.last_type; ++t)
+            if (nh_psi_of_type(d, sp, t)) return;
         if (d.mixed) phase_drift<true>(d, sp, true); else phase_drift<false>(d, sp, true);
     } else {
         if (d.mixed) phase_drift<true>(d, sp, false); else phase_drift<false>(d, sp, false);
     }
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_DRIFT);
     phase_decide(d, sp);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_DECIDE);
     if (*(volatile unsigned int*)(d.bar + 2) == 0u) return;
     if (clk.tr) atomicAdd(clk.tr + TR_REBUILD_LAUNCHES, 1ull);
@@ -1070,26 +1115,26 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
 // The rebuild phases of k_pre (replicas with their rebuild flag set).
 __device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp, PhaseClock& clk) {
     phase_zero_cells(d);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_ZERO);
     phase_bin(d);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_BIN);
     const int chunk = (d.ncells + gridDim.x - 1) / gridDim.x;
     phase_scan_a(d, chunk);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_SCAN_A);
     phase_scan_b(d);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_SCAN_B);
     phase_scan_c(d, chunk);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_SCAN_C);
     phase_scatter(d, !sp.do_drift);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_SCATTER);
     if (d.mixed) phase_sort_gather<true>(d, !sp.do_drift); else phase_sort_gather<false>(d, !sp.do_drift);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     clk.mark(TR_GATHER);
     if (clk.tr) clk.tr[TR_STAMP] = clk.last;
     // brute-mode replicas here; cell-mode replicas in k_build_list, which
@@ -1100,21 +1145,22 @@ __device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp
 // Macro parameters of type `sel` (solver/src/macro_parameters): results land
 // in the replica records (vcm, mom, ke, pe, thermal, T, P, count).
 __global__ void __launch_bounds__(TILE) k_macro(Dev d, StepParams sp, int sel) {
+    barrier_setup(sp);
     tile_rep_reset();
     if (d.refmode) {
         phase_serial(d, sp, sel, false);
         return;
     }
     phase_partials1(d, sel);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     phase_chunk_sums<7>(d);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     phase_finalize1(d, sel);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     phase_partials2(d, sel);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     phase_chunk_sums<1>(d);
-    grid_barrier(d);
+    if (grid_barrier(d)) return;
     phase_finalize2(d, sp, false, sel);
 }
 
@@ -1146,7 +1192,8 @@ __global__ void k_apply_pending_box(Dev d) {
     W->pending = 1.0;
 }
 
-// Device -> caller order (for download): out[orig[s]] = value[s].
+// Device -> caller order (for download): out[orig[s]] = value[s]; a null
+// output is skipped.
 __global__ void k_gather_out(Dev d, double* out_pos, double* out_vel, double* out_frc,
                              double* out_pot, double* out_tmp) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1154,26 +1201,32 @@ __global__ void k_gather_out(Dev d, double* out_pos, double* out_vel, double* ou
     if (s >= N) return;
     const int o = d.orig[s];
     if (o < 0 || o >= N) { atomicOr(d.err, E_BOUNDS); return; }
-    const double4_32a p = d.pos[s];
-    out_pos[3 * (size_t)o] = p.x; out_pos[3 * (size_t)o + 1] = p.y; out_pos[3 * (size_t)o + 2] = p.z;
-    for (int k = 0; k < 3; ++k) {
-        out_vel[3 * (size_t)o + k] = d.vel[(size_t)k * N + s];
-        out_frc[3 * (size_t)o + k] = d.frc[(size_t)k * N + s];
+    if (out_pos) {
+        const double4_32a p = d.pos[s];
+        out_pos[3 * (size_t)o] = p.x; out_pos[3 * (size_t)o + 1] = p.y; out_pos[3 * (size_t)o + 2] = p.z;
     }
-    out_pot[o] = d.epot[s];
-    out_tmp[o] = d.evir[s];
+    for (int k = 0; k < 3; ++k) {
+        if (out_vel) out_vel[3 * (size_t)o + k] = d.vel[(size_t)k * N + s];
+        if (out_frc) out_frc[3 * (size_t)o + k] = d.frc[(size_t)k * N + s];
+    }
+    if (out_pot) out_pot[o] = d.epot[s];
+    if (out_tmp) out_tmp[o] = d.evir[s];
 }
 
 // Caller order -> device (upload): the device order starts as the caller's;
-// the first rebuild sorts it by cell.
-__global__ void k_scatter_in(Dev d, const double* in_pos, const double* in_vel, const int* in_type,
-                             const int* in_rank) {
+// the first rebuild sorts it by cell.  in_rank null: one type, the rank is the
+// index.  A type id >= ntypes is flagged (E_INPUT) and replaced by 0, so no
+// later kernel indexes the pair table with it.
+__global__ void k_scatter_in(Dev d, const double* in_pos, const double* in_vel, const uint16_t* in_type,
+                             const int* in_rank, int ntypes) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = d.ntot;
     if (s >= N) return;
+    int ty = (int)in_type[s];
+    if (ty >= ntypes) { atomicOr(d.err, E_INPUT); ty = 0; }
     double4_32a p;
     p.x = in_pos[3 * (size_t)s]; p.y = in_pos[3 * (size_t)s + 1]; p.z = in_pos[3 * (size_t)s + 2];
-    p.w = __longlong_as_double((long long)in_type[s]);
+    p.w = __longlong_as_double((long long)ty);
     d.pos[s] = p;
     for (int k = 0; k < 3; ++k) {
         d.vel[(size_t)k * N + s] = in_vel ? in_vel[3 * (size_t)s + k] : 0.0;
@@ -1182,8 +1235,10 @@ __global__ void k_scatter_in(Dev d, const double* in_pos, const double* in_vel, 
     d.epot[s] = 0.0;
     d.evir[s] = 0.0;
     d.orig[s] = s;
-    d.rank[s] = in_rank[s];
-    d.slot_of_rank[in_rank[s]] = s;
+    int rk = in_rank ? in_rank[s] : s;
+    if (rk < 0 || rk >= N) { atomicOr(d.err, E_BOUNDS); rk = s; }
+    d.rank[s] = rk;
+    d.slot_of_rank[rk] = s;
     d.cell[s] = -1;
     d.nn[s] = 0;
     d.mir0[s] = make_float4(0.f, 0.f, 0.f, 0.f);

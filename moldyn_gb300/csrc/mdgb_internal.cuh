@@ -43,6 +43,7 @@ enum : int {
     E_SKIN = 8,       // fixed rebuild interval let an atom move too far
     E_BOUNDS = 16,    // an index derived from scratch data was out of range
     E_CELLS = 32,     // cell bookkeeping inconsistent
+    E_INPUT = 64,     // an uploaded type id >= ntypes
 };
 
 enum : int { MODE_CELLS = 0, MODE_BRUTE = 1 };
@@ -99,12 +100,15 @@ struct StepParams {
     int do_drift;              // 0: only (re)build / refresh, no integration
     int predrifted;            // the previous force pass already kicked and drifted (NVE)
     int fused;                 // force pass: also the next step's kick and drift (into pos_next/mir_next)
+    int hold_block;            // >= 0: that block of the step kernel enters its first grid barrier late
+                               //   (failure test of the bounded barrier; -1 in every normal step)
+    long long barrier_cycles;  // > 0: the grid barrier's wait limit in clock cycles (0: the default, ~2 s)
 };
 
 // Everything a kernel needs, passed by value.
 struct Dev {
     int ntot, ntiles, nrep, ntypes, cap, tpa, ncells;
-    int refmode, mixed, single_type, last_type;
+    int refmode, mixed, single_type, last_type, pad_dev;
     double mass[MAX_TYPES];
     double rlist, rcmax, skin;
     float fscale, inv_fscale_f;  // fixed-point scale 2^fscale_log2
@@ -161,6 +165,13 @@ enum : int {
     TR_STAMP = 15,   // time stamp the list-build kernel measures from
     TR_SLOTS = 16
 };
+
+// A failed grid barrier earlier in this chunk (E_TIMEOUT): the launches that
+// follow in the chunk do nothing (the engine restores the chunk's starting
+// state and reports MDGB_ERR_DEVICE_TIMEOUT).
+__device__ __forceinline__ bool chunk_failed(const Dev& d) {
+    return (*(volatile const int*)d.err & E_TIMEOUT) != 0;
+}
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;

@@ -197,18 +197,42 @@ class Engine:
         if barostat is not None:
             barostat.myu = ba.myu
 
-    def download(self):
+    def prepare_step(self, nsteps: int, dt: float, thermostat=None, barostat=None):
+        """Capture the CUDA graphs a later step(nsteps, dt, ...) with these
+        coupling kinds replays, without taking a step (graph_steps > 1)."""
+        th = ba = None
+        if thermostat is not None:
+            th = _lib.CThermostat(thermostat.kind_id, thermostat.tau, 0.0, thermostat.lambda_, thermostat.psi)
+        if barostat is not None:
+            ba = _lib.CBarostat(barostat.beta, barostat.tau, 0.0, barostat.myu)
+        if self.nrep > 1:
+            self._check(self._L.mdgb_ensemble_prepare(self._h, int(nsteps), float(dt)))
+        else:
+            self._check(self._L.mdgb_prepare_step(self._h, int(nsteps), float(dt),
+                                                  C.byref(th) if th is not None else None,
+                                                  C.byref(ba) if ba is not None else None))
+
+    def test_barrier_timeout(self, hold_block: int, wait_cycles: int):
+        """Arm the bounded-barrier failure test for the next step call."""
+        self._check(self._L.mdgb_test_barrier_timeout(self._h, int(hold_block), int(wait_cycles)))
+
+    def download(self, out: dict | None = None, fields=("pos", "vel", "force", "potential", "temp")):
+        """The state in the caller's atom order.  `out` may hold arrays to fill
+        (reused across calls); only `fields` are copied from the device."""
         n = self.n
-        out = {k: np.empty((n, 3)) for k in ("pos", "vel", "force")}
-        out["potential"] = np.empty(n)
-        out["temp"] = np.empty(n)
+        shapes = {"pos": (n, 3), "vel": (n, 3), "force": (n, 3), "potential": (n,), "temp": (n,)}
+        res = {} if out is None else out
+        for k in fields:
+            a = res.get(k)
+            if a is None or a.shape != shapes[k] or a.dtype != np.float64 or not a.flags.c_contiguous:
+                res[k] = np.empty(shapes[k])
         box = np.empty(3 * max(self.nrep, 1))
         fn = self._L.mdgb_download_state if self.nrep == 1 else self._L.mdgb_ensemble_download
-        self._check(fn(self._h, _lib.as_ptr(out["pos"]), _lib.as_ptr(out["vel"]),
-                       _lib.as_ptr(out["force"]), _lib.as_ptr(out["potential"]),
-                       _lib.as_ptr(out["temp"]), _lib.as_ptr(box)))
-        out["box"] = box[:3].copy() if self.nrep == 1 else box.reshape(-1, 3)
-        return out
+        ptr = {k: (_lib.as_ptr(res[k]) if k in fields else None) for k in shapes}
+        self._check(fn(self._h, ptr["pos"], ptr["vel"], ptr["force"], ptr["potential"], ptr["temp"],
+                       _lib.as_ptr(box)))
+        res["box"] = box[:3].copy() if self.nrep == 1 else box.reshape(-1, 3)
+        return res
 
     def macro(self, type_id: int = 0):
         m = (_lib.CMacro * max(self.nrep, 1))()

@@ -118,7 +118,15 @@ int oref_update_force(int ntypes, const int64_t* counts, const double* pos,
             const oref_lj pot = table_get(pot_table, ntypes, t1, t2);
             const double r_cut = pot.r_cut;
             int64_t ib = std::max(off[t1], row_begin), ie = std::min(off[t1 + 1], row_end);
-#pragma omp parallel for schedule(dynamic, 64)
+            // rows per scheduling chunk: small enough that a sampled row range
+            // keeps every thread busy (rows are independent: any schedule
+            // gives the same bits)
+            int nth = 1;
+#ifdef _OPENMP
+            nth = nthreads > 0 ? nthreads : omp_get_max_threads();
+#endif
+            const int64_t csize = std::max<int64_t>(1, std::min<int64_t>(64, (ie - ib) / (8 * (int64_t)nth)));
+#pragma omp parallel for schedule(dynamic, csize)
             for (int64_t gi = ib; gi < ie; ++gi) {
                 const int64_t i = gi - off[t1];
                 const double pix = pos[3 * gi], piy = pos[3 * gi + 1], piz = pos[3 * gi + 2];

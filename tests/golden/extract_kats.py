@@ -1,8 +1,8 @@
 """Extract the reference's golden test values into ``reference_kats.json``.
 
-Run here (where the reference source tree is mounted read-only):
+Run with the path of a checkout of the reference source tree (read only):
 
-    python tests/golden/extract_kats.py /root/reference
+    python tests/golden/extract_kats.py <path-to-moldyn-checkout>
 
 The reference is Rust and cannot be built or run in this environment, so its
 known-answer tests are read as text: every
@@ -105,4 +105,6 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/extract_kats.py <path-to-moldyn-checkout>")
+    main(sys.argv[1])

@@ -65,3 +65,27 @@ def test_headline_system_is_the_documented_workload():
     assert t_star == pytest.approx(0.72, rel=0.01)
     pos2, vel2, _ = bench.make_system(seed=1234)
     assert np.array_equal(pos, pos2) and np.array_equal(vel, vel2)
+
+
+def test_reference_arm_loads_no_product_code():
+    """The reference arm builds its system with the oracle and times the
+    oracle: the product package (and libmdgb.so) is never imported."""
+    code = ("import sys, argparse; sys.path.insert(0, %r); import bench; "
+            "bench.run_reference(argparse.Namespace(steps=1, warmup=3, gpus=1)); "
+            "bad = [m for m in sys.modules if m.startswith('moldyn_gb300')]; "
+            "assert not bad, bad" % ROOT)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][0])
+    # the timed region is what ran: the sampled step's own time
+    assert d["ms_per_step"] == pytest.approx(d["sampled_step"]["ms"])
+    assert d["sampled_step"]["full_step_ms_extrapolated"] > d["ms_per_step"]
+
+
+def test_reference_arm_positions_are_the_headline_system():
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    pos, vel, box = bench.make_system(seed=1234)
+    opos, obox = bench.make_positions_oracle()
+    assert np.array_equal(pos, opos) and np.array_equal(box, obox)

@@ -123,3 +123,26 @@ def test_trace_flag_and_phase_names():
     assert len(_lib.TRACE_PHASES) == 14 and _lib.TRACE_PHASES[-2:] == ["launches", "rebuild_launches"]
     src = open(os.path.join(ROOT, "include", "mdgb.h")).read()
     assert "#define MDGB_FLAG_TRACE 8u" in src
+
+
+def test_noalloc_validates_arguments_on_the_host(lib):
+    """mdgb_forces_noalloc rejects a box that is not positive and finite, and
+    a non-finite sigma, before any CUDA call (no device pointer is touched)."""
+    for box in ([np.inf, 10.0, 10.0], [10.0, np.nan, 10.0], [10.0, 10.0, -1.0], [0.0, 10.0, 10.0]):
+        assert lib.mdgb_forces_noalloc(10, 1, np.array(box), 1.0, 1.0, 1, None, None, None) == 1
+    assert lib.mdgb_forces_noalloc(10, 1, np.array([10.0, 10.0, 10.0]), np.nan, 1.0, 1, None, None, None) == 1
+    assert lib.mdgb_forces_noalloc(10, 1, np.array([10.0, 10.0, 10.0]), 1.0, np.inf, 1, None, None, None) == 1
+
+
+def test_noalloc_huge_box_grid_terminates_without_a_gpu(lib):
+    """A box of 1e12 passes validation; the cell grid is coarsened in closed
+    form (no per-cell loop), and without a GPU the call ends with a CUDA error
+    instead of launching anything."""
+    import time
+
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present (the GPU test covers this box with real buffers)")
+    t0 = time.perf_counter()
+    st = lib.mdgb_forces_noalloc(10, 1, np.array([1e12, 1e12, 1e12]), 1.0, 1.0, 1, None, None, None)
+    assert st == 2 and time.perf_counter() - t0 < 5.0
