@@ -70,9 +70,6 @@ __device__ __forceinline__ double ref_distance(const double4_32a pi, const doubl
 constexpr float FIX_MAGIC = 12582912.0f;           // 1.5 * 2^23
 constexpr unsigned FIX_MAGIC_BITS = 0x4B400000u;   // bits of FIX_MAGIC
 constexpr int FIX_FOLD = 256;                      // most terms per lane the words can hold
-#ifndef MDGB_PAIRED_LOOP
-#define MDGB_PAIRED_LOOP 0
-#endif
 
 struct FixAcc {
     unsigned hi, lo;
@@ -107,18 +104,6 @@ __device__ __forceinline__ void fix_add_xyz(FixAcc& ax, FixAcc& ay, FixAcc& az, 
     const float bz = fmaf(lz, 8388608.0f, FIX_MAGIC);
     az.hi += __float_as_uint(az_);
     az.lo += __float_as_uint(bz);
-}
-
-// Two terms per component at once: lane lo of each f2 is one candidate, hi
-// the other (both go to the same atom's accumulators).
-__device__ __forceinline__ void fix_add2(FixAcc& acc, f2_t t2) {
-    const f2_t M2 = f2(FIX_MAGIC, FIX_MAGIC);
-    const f2_t K2 = f2(8388608.0f, 8388608.0f);
-    const f2_t a2 = add2(t2, M2);
-    const f2_t l2 = sub2(t2, sub2(a2, M2));
-    const f2_t b2 = fma2(l2, K2, M2);
-    acc.hi += (unsigned)a2 + (unsigned)(a2 >> 32);
-    acc.lo += (unsigned)b2 + (unsigned)(b2 >> 32);
 }
 
 template <int TPA>
@@ -390,9 +375,6 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
     const float rl = (float)(d.rlist * 1.01);
     const float split_limit = 2097152.0f / rl;       // 2^44 / 2^23 / rlist
     const float range_limit = 4294967296.0f / rl;    // 2^55 / 2^23 / rlist
-    // one pair type and fixed-point sums: the hot loop takes its candidates two
-    // at a time through the paired instructions
-    constexpr bool PAIRED = SINGLE && !NAIVE && (MDGB_PAIRED_LOOP != 0);
     int iter = 0;
     for (;;) {
         const int t = next_tile(d, PERSIST, iter, &s_tile);
@@ -447,43 +429,6 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
                     lj_f32(P, r2, fs, u);
                     acc.add(dxy, dz, r2, fs, u, fscale_t);
                 };
-                // Two candidates through the paired FP32 instructions at once
-                // (one per half of every f2): displacement, r^2, LJ and the
-                // fixed-point split; a candidate outside r_cut adds a zero term
-                // (no branch: some lane of the warp is inside almost always).
-                const float slo = P0.rc2_lo, shi = P0.rc2_hi;
-                const f2_t xixx = f2(xi.x, xi.x), xiyy = f2(xi.y, xi.y), xizz = f2(xi.z, xi.z);
-                const f2_t sig2_2 = f2(P0.sig2, P0.sig2), eps24_2 = f2(P0.eps24, P0.eps24);
-                const f2_t eps4_2 = f2(P0.eps4, P0.eps4), ucut_2 = f2(-P0.ucut, -P0.ucut);
-                const f2_t m2_2 = f2(-2.0f, -2.0f), one_2 = f2(1.0f, 1.0f), mone_2 = f2(-1.0f, -1.0f);
-                const f2_t fst2 = f2(fscale_t, fscale_t);
-                f2_t pe2 = f2(0.f, 0.f), vr2 = f2(0.f, 0.f);
-                auto pair2 = [&](uint32_t ea, float4 xa, uint32_t eb, float4 xb) {
-                    const float4 sa = tab[ea >> IDX_BITS], sb = tab[eb >> IDX_BITS];
-                    const f2_t dx = add2(sub2(f2(xa.x, xb.x), xixx), f2(sa.x, sb.x));
-                    const f2_t dy = add2(sub2(f2(xa.y, xb.y), xiyy), f2(sa.y, sb.y));
-                    const f2_t dz = add2(sub2(f2(xa.z, xb.z), xizz), f2(sa.z, sb.z));
-                    const f2_t r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-                    const float r2a = f2_lo(r2), r2b = f2_hi(r2);
-                    band |= ((r2a >= slo) & (r2a <= shi)) | ((r2b >= slo) & (r2b <= shi));
-                    const f2_t r2i = f2(__fdividef(1.0f, r2a), __fdividef(1.0f, r2b));
-                    const f2_t s2 = mul2(sig2_2, r2i);
-                    const f2_t s6 = mul2(s2, mul2(s2, s2));
-                    f2_t fs = mul2(mul2(eps24_2, r2i), mul2(s6, fma2(m2_2, s6, one_2)));
-                    fs = f2(r2a < slo ? f2_lo(fs) : 0.0f, r2b < slo ? f2_hi(fs) : 0.0f);
-                    if (!NOE) {
-                        f2_t u = fma2(mul2(eps4_2, s6), add2(s6, mone_2), ucut_2);
-                        u = f2(r2a < slo ? f2_lo(u) : 0.0f, r2b < slo ? f2_hi(u) : 0.0f);
-                        pe2 = add2(pe2, u);
-                        vr2 = fma2(fs, r2, vr2);
-                    }
-                    const f2_t g = mul2(fs, fst2);
-                    acc.gmax = fmaxf(acc.gmax, fmaxf(fabsf(f2_lo(g)), fabsf(f2_hi(g))));
-                    fix_add2(acc.ax, mul2(dx, g));
-                    fix_add2(acc.ay, mul2(dy, g));
-                    fix_add2(acc.az, mul2(dz, g));
-                    acc.n += 2;
-                };
                 // this lane's entries k = lane, lane + TPA, ...: two per iteration,
                 // the next iteration's two list words already in flight (the list
                 // streams from HBM; the gathers hit L2)
@@ -500,20 +445,12 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
                     uint32_t na = 0u, nb = 0u;
                     if (i + 2 < m) na = __ldcs(lbase + (size_t)(i + 2) * lstride);
                     if (i + 3 < m) nb = __ldcs(lbase + (size_t)(i + 3) * lstride);
-                    if (PAIRED) {
-                        pair2(ea, xa, eb, xb);
-                    } else {
-                        pair(ea, xa);
-                        pair(eb, xb);
-                    }
+                    pair(ea, xa);
+                    pair(eb, xb);
                     ea = na;
                     eb = nb;
                 }
                 if (i < m) pair(ea, __ldg(d.mir + (ea & IDX_MASK)));
-                if (PAIRED && !NOE) {
-                    acc.pe += f2_lo(pe2) + f2_hi(pe2);
-                    acc.vr += f2_lo(vr2) + f2_hi(vr2);
-                }
                 deferred = band;
             } else {
                 // brute mode (a box smaller than three list radii): the reference's
