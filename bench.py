@@ -287,11 +287,15 @@ def run_ours(args):
     types = np.zeros(n, dtype=np.uint16)
 
     # ---- mixed path, state resident in HBM --------------------------------
+    # the headline leg is the mixed path; --legs mixed --precision fp64 times
+    # the plain FP64 path the same way (profiler captures)
+    leg_precision = args.precision if args.legs == "mixed" else "mixed"
+
     def timed_leg(**kw):
         """K steps from the seeded start after W warm-up steps: device time
         (CUDA events on the engine's stream, max over ranks), stats, clocks,
         end state."""
-        eng = Engine(precision="mixed", skin=SKIN, device=local, **kw)
+        eng = Engine(precision=leg_precision, skin=SKIN, device=local, **kw)
         eng.set_potential(0, 0, 1.0, 1.0)
         eng.upload(types, pos, vel, [1.0], box)
         eng.compute_forces()
@@ -339,7 +343,8 @@ def run_ours(args):
             phases = te.trace_phases()
             te.close()
         if rank == 0:
-            print(json.dumps({"legs": "mixed", "value": value, "ms_per_step": t_ms / args.steps,
+            print(json.dumps({"legs": "mixed", "precision": leg_precision, "value": value,
+                              "ms_per_step": t_ms / args.steps,
                               "eager_profiled_ms_per_step": t_prof / args.steps,
                               "force_kernel_ms": force_ms_avg, "threads_per_atom": st.threads_per_atom,
                               "rebuilds": st.rebuilds, "clocks": clocks, "k_pre_phases_us": phases}), flush=True)
@@ -659,8 +664,10 @@ def run_ensemble(args):
     n, nrep = len(pos), len(offs) - 1
     t0s = tst * 100.0 / K_B
     res = {}
-    for prec in ("mixed", "fp64"):
-        e = Engine(precision=prec, skin=SKIN, persistent=True, graph_steps=50)
+    # the mixed path with the skin chosen per size class by the engine, then
+    # the same with the fixed 0.3 sigma skin, and the plain FP64 path
+    for leg, prec, skin in (("mixed", "mixed", 0.0), ("mixed_fixed_skin", "mixed", SKIN), ("fp64", "fp64", SKIN)):
+        e = Engine(precision=prec, skin=skin, persistent=True, graph_steps=50)
         e.set_potential(0, 0, 1.0, 1.0)
         e.upload_ensemble(offs, np.zeros(n, dtype=np.uint16), pos, vel, [1.0], boxes)
         e.compute_forces()
@@ -668,18 +675,22 @@ def run_ensemble(args):
         bas = [Barostat.Berendsen(1.0, 5.0) for _ in range(nrep)]
         e.ensemble_set_coupling(ths, t0s, bas, p0)
         steps = args.steps if prec == "mixed" else max(50, min(args.steps, args.fp64_steps or 50))
-        e.ensemble_step(50, DT)            # warm-up, graph capture
+        e.ensemble_step(50, DT)            # warm-up (and skin tuning), graph capture
+        e.prepare_step(steps, DT)
         e.reset_stats()
         if dist is not None:
             dist.barrier()
         ms = max_over_ranks(_timed_steps(e, steps, DT, ensemble=True), dist, "cuda")
         st = e.stats()
-        res[prec] = {"value": n_all * steps / (ms * 1e-3), "steps": steps, "ms_per_step": ms / steps,
-                     "graph_launches": st.graph_launches, "rebuilds": st.rebuilds,
-                     "threads_per_atom_by_size_class": {"<2048": st.class_threads_per_atom[0],
-                                                        "2048-32767": st.class_threads_per_atom[1],
-                                                        ">=32768": st.class_threads_per_atom[2]},
-                     "replicas_by_size_class": list(st.class_replicas)}
+        res[leg] = {"value": n_all * steps / (ms * 1e-3), "steps": steps, "ms_per_step": ms / steps,
+                    "graph_launches": st.graph_launches, "rebuilds": st.rebuilds,
+                    "threads_per_atom_by_size_class": {"<2048": st.class_threads_per_atom[0],
+                                                       "2048-32767": st.class_threads_per_atom[1],
+                                                       ">=32768": st.class_threads_per_atom[2]},
+                    "skin_sigma_by_size_class": {"<2048": st.class_skin[0], "2048-32767": st.class_skin[1],
+                                                 ">=32768": st.class_skin[2]},
+                    "skin": "tuned per size class" if skin <= 0 else f"fixed {skin}",
+                    "replicas_by_size_class": list(st.class_replicas)}
         e.close()
     if rank != 0:
         return
@@ -690,7 +701,8 @@ def run_ensemble(args):
                        "replicas_on_rank0": nrep,
                        "atoms_min_max_mean": [int(ns.min() ** 3), int(ns.max() ** 3), float((ns ** 3).mean())],
                        "graph_steps": 50, "persistent_force_kernel": True,
-                       "mixed": res["mixed"], "fp64_plain_path": res["fp64"],
+                       "mixed": res["mixed"], "mixed_fixed_skin": res["mixed_fixed_skin"],
+                       "fp64_plain_path": res["fp64"],
                        "mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"]}}
     print(json.dumps(line), flush=True)
 
@@ -799,6 +811,8 @@ def main():
     ap.add_argument("--legs", default="all", choices=["all", "mixed"],
                     help="'mixed' runs only the timed mixed leg (for profiler captures)")
     ap.add_argument("--trace", action="store_true", help="with --legs mixed: per-phase times of the step kernel")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="with --legs mixed: the path whose steps are timed (profiler captures)")
     ap.add_argument("--tpa", type=int, default=0, help="threads per atom of the lj1m mixed leg (0: autotune)")
     ap.add_argument("--graph-steps", type=int, default=64,
                     help="lj1m: time the mixed path with chunks of this many steps replayed as CUDA graphs "

@@ -71,7 +71,8 @@ class CStats(C.Structure):
                 ("max_neighbors", C.c_int), ("threads_per_atom", C.c_int), ("retries", C.c_int),
                 ("force_ms", C.c_double), ("force_launches", C.c_int64),
                 ("integrate_ms", C.c_double), ("integrate_launches", C.c_int64),
-                ("class_threads_per_atom", C.c_int * 3), ("class_replicas", C.c_int * 3)]
+                ("class_threads_per_atom", C.c_int * 3), ("class_replicas", C.c_int * 3),
+                ("class_skin", C.c_double * 3)]
 
 
 class CSplatParams(C.Structure):

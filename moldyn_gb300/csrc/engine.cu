@@ -92,6 +92,11 @@ struct mdgb_engine {
     int class_ntiles[NCLASS] = {0, 0, 0};
     int class_tile_off[NCLASS] = {0, 0, 0};   // offset into dev.tile_order
     int class_nrep[NCLASS] = {0, 0, 0};
+    // Verlet skin of each size class (a replica's list radius is the largest
+    // r_cut plus its class's skin): the configured skin, or tuned on the
+    // first step call when the configuration leaves it to the engine
+    double class_skin[NCLASS] = {0.0, 0.0, 0.0};
+    bool skin_tuned = false;
 
     Dev dev{};
     // allocations
@@ -200,6 +205,28 @@ const LJ& pot_of(const mdgb_engine* e, int a, int b) {
     return e->pot[a][b].set ? e->pot[a][b] : e->pot_default;
 }
 
+// Skin of size class c: the tuned one, else the configured (or default) one.
+double class_skin_of(const mdgb_engine* e, int c) { return e->skin_tuned ? e->class_skin[c] : e->skin; }
+
+// The configuration leaves the skin to the engine (reference-order runs keep
+// the default: their sums do not depend on the list).
+bool skin_auto(const mdgb_engine* e) {
+    return !(e->cfg.skin > 0.0) && !((e->cfg.flags & MDGB_FLAG_REFERENCE_ORDER) && e->cfg.precision == MDGB_PRECISION_FP64);
+}
+
+// Skin candidates of the tuning, as fractions of the largest r_cut
+// (0.2 .. 0.4 sigma at r_cut = 2.5 sigma).
+constexpr double SKIN_FRACTIONS[5] = {0.08, 0.10, 0.12, 0.14, 0.16};
+
+// The largest list radius of any replica (the force kernels' range bounds).
+void update_rlist(mdgb_engine* e) {
+    double smax = e->skin;
+    for (int c = 0; c < mdgb_engine::NCLASS; ++c)
+        if (e->class_ntiles[c]) smax = std::max(smax, class_skin_of(e, c));
+    e->rlist = e->rcmax + smax;
+    e->dev.rlist = e->rlist;
+}
+
 // The pair table of the current potentials and the scalars derived from it
 // (largest cut-off, list radius, fixed-point scale), on the host.
 std::vector<PairDev> pair_table(mdgb_engine* e) {
@@ -235,8 +262,7 @@ std::vector<PairDev> pair_table(mdgb_engine* e) {
     e->dev.inv_fscale = std::ldexp(1.0, -ex);
     e->dev.inv_fscale_f = std::ldexp(1.0f, -ex);
     e->skin = e->cfg.skin > 0.0 ? e->cfg.skin : 0.12 * e->rcmax;
-    e->rlist = e->rcmax + e->skin;
-    e->dev.rlist = e->rlist;
+    update_rlist(e);
     e->dev.rcmax = e->rcmax;
     e->dev.skin = e->skin;
     return tab;
@@ -404,6 +430,17 @@ int apply_class_tpa(mdgb_engine* e) {
     if (!changed) return MDGB_OK;
     CU(cudaMemcpyAsync(e->dev.rep, e->rep_host.data(), e->nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
     e->lists_fresh = false;   // the list layout changed
+    return MDGB_OK;
+}
+
+// Each replica's list radius: the largest r_cut plus its size class's skin.
+int apply_class_skin(mdgb_engine* e) {
+    CU(cudaMemcpyAsync(e->rep_host.data(), e->dev.rep, e->nrep * sizeof(RepDev), cudaMemcpyDeviceToHost, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    for (int r = 0; r < e->nrep; ++r) e->rep_host[r].rlist = e->rcmax + class_skin_of(e, e->class_of[r]);
+    CU(cudaMemcpyAsync(e->dev.rep, e->rep_host.data(), e->nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
+    update_rlist(e);
+    e->lists_fresh = false;
     return MDGB_OK;
 }
 
@@ -659,12 +696,17 @@ int run_chunk(mdgb_engine* e, const StepParams& sp, int n) {
 int chunk_steps(const mdgb_engine* e) { return e->cfg.graph_steps > 1 ? e->cfg.graph_steps : 64; }
 
 int autotune_tpa(mdgb_engine* e);
+int autotune_skin(mdgb_engine* e, double dt);
 
 int step_impl(mdgb_engine* e, int64_t nsteps, double dt) {
     if (!e->has_state) return fail(e, MDGB_ERR_NO_STATE, "no state uploaded");
     if (nsteps < 0 || !(dt == dt)) return fail(e, MDGB_ERR_INVALID_ARGUMENT, "bad nsteps or dt");
     if (!e->tuned) {
         int rc = autotune_tpa(e);
+        if (rc) return rc;
+    }
+    if (nsteps > 0 && !e->skin_tuned && skin_auto(e)) {
+        int rc = autotune_skin(e, dt);
         if (rc) return rc;
     }
     const StepParams sp = make_sp(e, dt, true);
@@ -745,6 +787,13 @@ int prepare_impl(mdgb_engine* e, int64_t nsteps, double dt, bool thermo_on, bool
         if (rc) return rc;
     }
     const bool t0 = e->thermo_on, b0 = e->baro_on, n0 = e->thermo_nh;
+    if (nsteps > 0 && !e->skin_tuned && skin_auto(e)) {
+        // the tuning runs steps: with the coupling kinds of the later call
+        e->thermo_on = thermo_on; e->baro_on = baro_on; e->thermo_nh = thermo_nh;
+        const int rc = autotune_skin(e, dt);
+        e->thermo_on = t0; e->baro_on = b0; e->thermo_nh = n0;
+        if (rc) return rc;
+    }
     e->thermo_on = thermo_on; e->baro_on = baro_on; e->thermo_nh = thermo_nh;
     const StepParams sp = make_sp(e, dt, true);
     e->thermo_on = t0; e->baro_on = b0; e->thermo_nh = n0;
@@ -757,6 +806,79 @@ int prepare_impl(mdgb_engine* e, int64_t nsteps, double dt, bool thermo_on, bool
         if (rc) return rc;
     }
     return MDGB_OK;
+}
+
+// Skin of each size class, for the step's own dynamics: from the state the
+// first step call starts from, each candidate (SKIN_FRACTIONS of the largest
+// r_cut) runs a short stretch of steps (eager launches, CUDA-event timed, its
+// rebuilds included) and the state is put back; classes are tuned one after
+// the other, each keeping its fastest.  A larger skin means longer lists but
+// fewer rebuilds.  The steps taken here are not counted and leave no trace:
+// the state afterwards is the one the call started from.
+int autotune_skin(mdgb_engine* e, double dt) {
+    constexpr int NC = mdgb_engine::NCLASS;
+    constexpr int K = 40;
+    for (int c = 0; c < NC; ++c) e->class_skin[c] = e->skin;
+    e->skin_tuned = true;   // class_skin now holds the values in use
+    const unsigned saved_flags = e->cfg.flags;
+    const int64_t launches0 = e->st.kernel_launches;
+    e->cfg.flags &= ~MDGB_FLAG_PROFILE;
+    const StepParams sp = make_sp(e, dt, true);
+    int rc = snapshot(e, false);   // the state the call started from
+    unsigned long long trace0[TR_SLOTS];   // the tuning's steps stay out of the phase trace
+    if (!rc) {
+        CU(cudaMemcpyAsync(trace0, e->trace_buf, sizeof(trace0), cudaMemcpyDeviceToHost, e->stream));
+        CU(cudaStreamSynchronize(e->stream));
+    }
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (!rc && (cudaEventCreate(&ev[0]) != cudaSuccess || cudaEventCreate(&ev[1]) != cudaSuccess))
+        rc = fail(e, MDGB_ERR_CUDA, "cudaEventCreate failed");
+    for (int c = 0; c < NC && !rc; ++c) {
+        if (!e->class_ntiles[c]) continue;
+        float best = 1e30f;
+        double best_skin = e->class_skin[c];
+        for (int k = 0; k < 5 && !rc; ++k) {
+            e->class_skin[c] = SKIN_FRACTIONS[k] * e->rcmax;
+            bool done = false;
+            for (int attempt = 0; attempt < 8 && !done && !rc; ++attempt) {
+                rc = snapshot(e, true);
+                if (!rc) rc = apply_class_skin(e);
+                if (!rc) rc = rebuild_lists(e);
+                if (!rc) rc = clear_err(e);
+                if (rc) break;
+                if (cudaEventRecord(ev[0], e->stream) != cudaSuccess) { rc = fail(e, MDGB_ERR_CUDA, "event"); break; }
+                rc = run_chunk_kernels(e, sp, K);
+                if (rc) break;
+                if (cudaEventRecord(ev[1], e->stream) != cudaSuccess) { rc = fail(e, MDGB_ERR_CUDA, "event"); break; }
+                int flags = 0;
+                rc = read_err(e, &flags);
+                if (rc) break;
+                if (flags & E_NLIST) {   // longer lists: grow and time this candidate again
+                    rc = grow_list(e);
+                    continue;
+                }
+                rc = check_flags(e, flags);
+                if (rc) break;
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, ev[0], ev[1]) != cudaSuccess) { rc = fail(e, MDGB_ERR_CUDA, "event"); break; }
+                if (ms < best) { best = ms; best_skin = e->class_skin[c]; }
+                done = true;
+            }
+        }
+        e->class_skin[c] = best_skin;
+    }
+    for (auto& x : ev)
+        if (x) cudaEventDestroy(x);
+    e->cfg.flags = saved_flags;
+    e->st.kernel_launches = launches0;
+    if (rc) return rc;
+    // back to the starting state; its lists are rebuilt with the chosen skins
+    // (a real rebuild, counted and traced like any other)
+    CU(cudaMemcpyAsync(e->trace_buf, trace0, sizeof(trace0), cudaMemcpyHostToDevice, e->stream));
+    rc = snapshot(e, true);
+    if (!rc) rc = apply_class_skin(e);
+    if (!rc) rc = rebuild_lists(e);
+    return rc;
 }
 
 // Threads per atom for each size class: every candidate is timed on every
@@ -903,7 +1025,10 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     e->dev.ntypes = ntypes;
     const std::vector<PairDev> pair_tab = pair_table(e);
 
-    // tiles and cells
+    // tiles and cells (cell capacity for the smallest list radius the skin
+    // tuning may choose)
+    const bool auto_skin = skin_auto(e);
+    const double rl_cells = e->rcmax + (auto_skin ? std::min(e->skin, SKIN_FRACTIONS[0] * e->rcmax) : e->skin);
     std::vector<int4> tiles;
     std::vector<int> cell_rep;
     int max_rep_n = 0;
@@ -921,7 +1046,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         for (int a = 0; a < 3; ++a) {
             const double L = boxes[3 * r + a];
             R.box[a] = L; R.box_build[a] = L; R.cs[a] = L; R.inv_cs[a] = 1.0 / L; R.nc[a] = 1;
-            prod *= std::max(1.0, std::floor(L / (e->rlist * (1.0 + 1e-6))));
+            prod *= std::max(1.0, std::floor(L / (rl_cells * (1.0 + 1e-6))));
         }
         const double vol = boxes[3 * r] * boxes[3 * r + 1] * boxes[3 * r + 2];
         max_density = std::max(max_density, nr / vol);
@@ -983,6 +1108,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     for (int c = 0; c < NC; ++c)
         same_classes = same_classes && class_ntiles[c] == e->class_ntiles[c] && class_nrep[c] == e->class_nrep[c];
     if (!reuse) free_state(e);
+    if (!same_classes) e->skin_tuned = false;
     e->has_state = false;
     e->forces_valid = false;
     e->lists_fresh = false;
@@ -1058,7 +1184,11 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         for (int c = 0; c < NC; ++c) e->class_tpa[c] = t0;
         e->tuned = false;
     }
-    for (int r = 0; r < nrep; ++r) e->rep_host[r].tpa = e->class_tpa[e->class_of[r]];
+    for (int r = 0; r < nrep; ++r) {
+        e->rep_host[r].tpa = e->class_tpa[e->class_of[r]];
+        e->rep_host[r].rlist = e->rcmax + class_skin_of(e, e->class_of[r]);
+    }
+    update_rlist(e);
     e->tpa = e->class_tpa[0];
     for (int c = NC - 1; c >= 0; --c)
         if (e->class_ntiles[c]) { e->tpa = e->class_tpa[c]; break; }
@@ -1323,7 +1453,10 @@ static int set_pot(mdgb_engine* e, uint16_t t0, uint16_t t1, const LJ& p) {
         CU(cudaMemcpyAsync(e->rep_host.data(), e->dev.rep, e->nrep * sizeof(RepDev), cudaMemcpyDeviceToHost,
                            e->stream));
         CU(cudaStreamSynchronize(e->stream));
-        for (auto& R : e->rep_host) R.rebuild = 1;
+        for (int r = 0; r < e->nrep; ++r) {
+            e->rep_host[r].rebuild = 1;
+            e->rep_host[r].rlist = e->rcmax + class_skin_of(e, e->class_of[r]);
+        }
         CU(cudaMemcpyAsync(e->dev.rep, e->rep_host.data(), e->nrep * sizeof(RepDev), cudaMemcpyHostToDevice,
                            e->stream));
     }
@@ -1530,6 +1663,7 @@ MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out) {
     for (int c = 0; c < mdgb_engine::NCLASS; ++c) {
         e->st.class_threads_per_atom[c] = e->class_tpa[c];
         e->st.class_replicas[c] = e->class_nrep[c];
+        e->st.class_skin[c] = class_skin_of(e, c);
     }
     *out = e->st;
     return MDGB_OK;

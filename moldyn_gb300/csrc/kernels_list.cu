@@ -17,8 +17,9 @@
 // entry t of their atoms in the same pass, so in the [k / tpa][atom][k % tpa]
 // layout the stores of a pass are contiguous.
 //
-// A pair is listed when its FP32 distance is below rlist (1 + 1e-5): a
-// superset of the pairs inside rlist, which the force kernels decide exactly.
+// A pair is listed when its FP32 distance is below its replica's rlist
+// (1 + 1e-5): a superset of the pairs inside rlist, which the force kernels
+// decide exactly.
 #include <algorithm>
 
 #include "mdgb_internal.cuh"
@@ -70,13 +71,13 @@ __global__ void __launch_bounds__(LB_WARPS * 32, 11) k_build_list(Dev d) {
     int* own_t = reinterpret_cast<int*>(own_z + 16);
     float4* tab = reinterpret_cast<float4*>(own_t + 32);
     const int cap = d.cap;
-    const float rl = (float)(d.rlist * (1.0 + 1e-5));
-    const float rl2 = rl * rl;
     const int gw = blockIdx.x * LB_WARPS + wib, nw = gridDim.x * LB_WARPS;
     for (int c = gw; c < d.ncells; c += nw) {
         const int r = d.cell_rep[c];
         const RepDev* W = d.rep + r;
         if (!W->rebuild || W->mode != MODE_CELLS) continue;
+        const float rl = (float)(W->rlist * (1.0 + 1e-5));
+        const float rl2 = rl * rl;
         const int nc[3] = {W->nc[0], W->nc[1], W->nc[2]};
         const int base = W->cell_base;
         const int local = c - base;

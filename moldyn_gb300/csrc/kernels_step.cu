@@ -920,12 +920,12 @@ __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
 __device__ void phase_build_list(const Dev& d) {
     __shared__ int smi[32];
     const int cap = d.cap;
-    const float rl = (float)(d.rlist * (1.0 + 1e-5));
-    const float rl2 = rl * rl;
     for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
         const int4 tl = d.tiles[t];
         const RepDev& R = tile_rep(d, tl.x);
         if (!R.rebuild || R.mode == MODE_CELLS) continue;  // cell-mode replicas: k_build_list
+        const float rl = (float)(R.rlist * (1.0 + 1e-5));
+        const float rl2 = rl * rl;
         const int s = tl.y + threadIdx.x;
         const int tpa = R.tpa;
         int cnt = 0;

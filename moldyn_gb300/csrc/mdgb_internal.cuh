@@ -78,6 +78,7 @@ struct RepDev {
     double th_tau, th_T0, lambda, psi;
     double ba_beta, ba_tau, ba_P0, myu;
     double pending;        // barostat factor still to apply to positions (1 = none)
+    double rlist;          // list radius: the largest r_cut + this replica's skin (its size class's)
     // rebuild bookkeeping
     unsigned int max_disp_bits;
     int rebuild;
@@ -110,7 +111,7 @@ struct Dev {
     int ntot, ntiles, nrep, ntypes, cap, tpa, ncells;
     int refmode, mixed, single_type, last_type, pad_dev;
     double mass[MAX_TYPES];
-    double rlist, rcmax, skin;
+    double rlist, rcmax, skin;   // rlist: the largest list radius of any replica
     float fscale, inv_fscale_f;  // fixed-point scale 2^fscale_log2
     double inv_fscale;
     int fscale_log2, pad_fs;
@@ -399,21 +400,22 @@ __device__ __forceinline__ RepDev load_rep(const RepDev* p) {
 // 2*maxd, which must stay above the largest cutoff.  Explicit FP64
 // intrinsics: the step kernel and the fused force pass decide alike.
 __device__ __forceinline__ bool rebuild_needed(const Dev& d, const StepParams& sp, int steps_since0, int rebuild,
-                                               double box0, double box_build0, unsigned max_disp_bits) {
+                                               double box0, double box_build0, unsigned max_disp_bits,
+                                               double rlist) {
     const int steps_since = steps_since0 + (sp.do_drift ? 1 : 0);
     const double sc = __ddiv_rn(box0, box_build0);
     const double maxd = (double)__uint_as_float(max_disp_bits);
-    const double limit = __dsub_rn(__dsub_rn(__dmul_rn(sc, d.rlist), d.rcmax), __dmul_rn(1e-5, d.rlist));
+    const double limit = __dsub_rn(__dsub_rn(__dmul_rn(sc, rlist), d.rcmax), __dmul_rn(1e-5, rlist));
     return sp.force_rebuild || rebuild || (__dmul_rn(2.0, maxd) > limit) ||
            (sp.fixed_interval > 0 && steps_since >= sp.fixed_interval);
 }
 __device__ __forceinline__ bool rebuild_needed(const Dev& d, const StepParams& sp, const RepDev& R) {
-    return rebuild_needed(d, sp, R.steps_since, R.rebuild, R.box[0], R.box_build[0], R.max_disp_bits);
+    return rebuild_needed(d, sp, R.steps_since, R.rebuild, R.box[0], R.box_build[0], R.max_disp_bits, R.rlist);
 }
 // the same test reading only the fields it needs (through L2)
 __device__ __forceinline__ bool rebuild_needed_at(const Dev& d, const StepParams& sp, const RepDev* p) {
     return rebuild_needed(d, sp, __ldcg(&p->steps_since), __ldcg(&p->rebuild), __ldcg(&p->box[0]),
-                          __ldcg(&p->box_build[0]), __ldcg(&p->max_disp_bits));
+                          __ldcg(&p->box_build[0]), __ldcg(&p->max_disp_bits), __ldcg(&p->rlist));
 }
 
 __device__ __forceinline__ void decide_replica(const Dev& d, const StepParams& sp, int r) {
@@ -428,7 +430,7 @@ __device__ __forceinline__ void decide_replica(const Dev& d, const StepParams& s
     if (need) {
         long long nc[3];
         bool brute = R.cell_cap < 27;
-        const double cmin = __dmul_rn(d.rlist, 1.0 + 1e-6);
+        const double cmin = __dmul_rn(R.rlist, 1.0 + 1e-6);
         for (int a = 0; a < 3; ++a) {
             nc[a] = (long long)floor(__ddiv_rn(R.box[a], cmin));
             if (nc[a] < 3) brute = true;

@@ -41,6 +41,7 @@ class Stats:
     integrate_launches: int = 0
     class_threads_per_atom: tuple = (0, 0, 0)
     class_replicas: tuple = (0, 0, 0)
+    class_skin: tuple = (0.0, 0.0, 0.0)
     extra: dict = field(default_factory=dict)
 
 
@@ -92,6 +93,9 @@ class Engine:
         self.n = 0
         self.nrep = 0
         self.ntypes = 0
+        # macro parameters per type, kept until the state changes: the
+        # reference's getters (one per quantity) then cost one reduction
+        self._macro_cache = {}
 
     # -- lifecycle ------------------------------------------------------
     def close(self):
@@ -124,13 +128,16 @@ class Engine:
 
     # -- potentials -----------------------------------------------------
     def set_potential(self, t0: int, t1: int, sigma: float, eps: float):
+        self._macro_cache.clear()
         self._check(self._L.mdgb_set_potential(self._h, t0, t1, sigma, eps))
 
     def set_potential_raw(self, t0: int, t1: int, sigma: float, eps: float, r_cut: float, u_cut: float):
+        self._macro_cache.clear()
         self._check(self._L.mdgb_set_potential_raw(self._h, t0, t1, sigma, eps, r_cut, u_cut))
 
     # -- state ----------------------------------------------------------
     def upload(self, types, pos, vel, mass_per_type, box):
+        self._macro_cache.clear()
         types = np.ascontiguousarray(types, dtype=np.uint16)
         n = len(types)
         pos = _f64(pos, (n, 3))
@@ -142,6 +149,7 @@ class Engine:
         self.n, self.nrep, self.ntypes = n, 1, len(mass)
 
     def upload_ensemble(self, offsets, types, pos, vel, mass_per_type, boxes):
+        self._macro_cache.clear()
         offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         types = np.ascontiguousarray(types, dtype=np.uint16)
         n = len(types)
@@ -155,6 +163,7 @@ class Engine:
         self.n, self.nrep, self.ntypes = n, nrep, len(mass)
 
     def upload_forces(self, force=None, potential=None, temp=None):
+        self._macro_cache.clear()
         n = self.n
         f = None if force is None else _f64(force, (n, 3))
         p = None if potential is None else _f64(potential).reshape(n)
@@ -175,6 +184,7 @@ class Engine:
         return ii[:k], jj[:k]
 
     def compute_forces(self):
+        self._macro_cache.clear()
         self._check(self._L.mdgb_compute_forces(self._h))
 
     def step(self, nsteps: int, dt: float, thermostat=None, target_temperature: float = 0.0,
@@ -182,6 +192,7 @@ class Engine:
         """Integrator::VerletMethod.calculate `nsteps` times.  thermostat /
         barostat are initializer.Thermostat / Barostat objects whose coupling
         state (lambda, psi, myu) is updated in place."""
+        self._macro_cache.clear()
         th = ba = None
         if thermostat is not None:
             th = _lib.CThermostat(thermostat.kind_id, thermostat.tau, target_temperature,
@@ -235,6 +246,11 @@ class Engine:
         return res
 
     def macro(self, type_id: int = 0):
+        key = int(type_id)
+        if key in self._macro_cache:
+            hit = self._macro_cache[key]
+            return ({k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in hit.items()} if self.nrep == 1
+                    else [{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in x.items()} for x in hit])
         m = (_lib.CMacro * max(self.nrep, 1))()
         fn = self._L.mdgb_macro_parameters if self.nrep == 1 else self._L.mdgb_ensemble_macro
         self._check(fn(self._h, int(type_id), m))
@@ -242,7 +258,9 @@ class Engine:
                     thermal_energy=x.thermal_energy, temperature=x.temperature,
                     pressure=x.pressure, com_velocity=np.array(list(x.com_velocity)),
                     momentum=np.array(list(x.momentum)), count=int(x.count)) for x in m]
-        return res[0] if self.nrep == 1 else res
+        out = res[0] if self.nrep == 1 else res
+        self._macro_cache[key] = out
+        return self.macro(key)
 
     # -- ensembles --------------------------------------------------------
     def ensemble_set_coupling(self, thermostats=None, target_temperatures=None, barostats=None,
@@ -263,6 +281,7 @@ class Engine:
         self._coupling = (thermostats, th, barostats, ba)
 
     def ensemble_step(self, nsteps: int, dt: float):
+        self._macro_cache.clear()
         self._check(self._L.mdgb_ensemble_step(self._h, int(nsteps), float(dt)))
 
     def ensemble_get_coupling(self):

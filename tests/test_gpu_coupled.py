@@ -340,3 +340,70 @@ def test_nose_hoover_two_types_vs_oracle(Engine, oracle, precision, ref, tol):
         assert dpos <= tol and dvel <= tol * 10
     assert oth.psi != 0.0
     e.close()
+
+
+# --------------------------------------------------------------------------
+# skin tuning
+
+def test_skin_tuning_leaves_no_trace(Engine):
+    """skin <= 0: the first step call times a short stretch of steps with each
+    candidate skin (0.08 .. 0.16 of r_cut) and puts the state back.  The run
+    then equals, bit for bit, engines configured with the chosen skins (the
+    same cell grids and lists) that start from the same forces -- those the
+    tuned engine's compute_forces left, which the first kick uses -- on an
+    ensemble with two size classes, replica by replica."""
+    systems = [gs.fcc((5, 5, 5), jitter=0.04, seed=111), gs.fcc((9, 9, 9), jitter=0.04, seed=112)]
+    offs = np.cumsum([0] + [len(s[0]) for s in systems])
+    pos = np.concatenate([s[0] for s in systems])
+    vel = np.concatenate([s[1] for s in systems])
+    boxes = np.array([s[2] for s in systems])
+    types = np.zeros(len(pos), dtype=np.uint16)
+    a = Engine(precision="mixed", threads_per_atom=1)
+    a.set_potential(0, 0, 1.0, 1.0)
+    a.upload_ensemble(offs, types, pos, vel, [1.0], boxes)
+    a.compute_forces()
+    f0 = a.download()
+    a.ensemble_step(30, DT)
+    got = a.download()
+    st = a.stats()
+    a.close()
+    cands = [f * 2.5 for f in (0.08, 0.10, 0.12, 0.14, 0.16)]
+    present = [c for c in range(3) if st.class_replicas[c]]
+    assert present == [0, 1]
+    for c in present:
+        assert min(abs(st.class_skin[c] - x) for x in cands) < 1e-12, st.class_skin
+    print("tuned skins:", st.class_skin)
+    for r, (p, v, bx) in enumerate(systems):
+        sl = slice(offs[r], offs[r + 1])
+        f = Engine(precision="mixed", threads_per_atom=1, skin=st.class_skin[r])
+        f.set_potential(0, 0, 1.0, 1.0)
+        f.upload(np.zeros(len(p), dtype=np.uint16), p, v, [1.0], bx)
+        f.upload_forces(f0["force"][sl], f0["potential"][sl], f0["temp"][sl])
+        f.step(30, DT)
+        w = f.download()
+        f.close()
+        for k in ("pos", "vel", "force"):
+            assert np.array_equal(got[k][sl], w[k]), (r, k)
+
+
+def test_macro_getters_share_one_reduction(Engine):
+    """The reference's getters (one per quantity, mod.rs / energy.rs /
+    pressure.rs) read one cached reduction until the state changes."""
+    from moldyn_gb300 import macro_parameters as mp
+    from moldyn_gb300.core import ParticleDatabase, State
+    from moldyn_gb300.solver import PotentialsDatabase, set_precision, update_force
+    set_precision("mixed")
+    ParticleDatabase.add(0, "test_particle", 1.0, 0.1)
+    pos, vel, box = gs.fcc((4, 4, 4), jitter=0.03, seed=121)
+    st = State(pos, vel, [0] * len(pos), box)
+    update_force(PotentialsDatabase(), st)
+    eng = st._engine
+    n0 = eng.stats().kernel_launches
+    vals = [mp.get_kinetic_energy(st, 0), mp.get_thermal_energy(st, 0), mp.get_potential_energy(st, 0),
+            mp.get_pressure(st, 0), mp.get_center_of_mass_velocity(st, 0), mp.get_momentum_of_system(st, 0)]
+    assert eng.stats().kernel_launches - n0 == 1
+    m = eng.macro(0)
+    assert vals[0] == m["kinetic_energy"] and vals[3] == m["pressure"]
+    eng.step(1, DT)
+    assert mp.get_kinetic_energy(st, 0) == eng.macro(0)["kinetic_energy"]
+    set_precision("fp64")

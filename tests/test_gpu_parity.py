@@ -596,7 +596,7 @@ def test_trace_phases_account_for_the_step_kernel(mdgb):
     """MDGB_FLAG_TRACE: per-phase device time of the step kernel; launch and
     rebuild counts match the steps taken and the rebuild statistics."""
     pos, vel, box = gs.fcc((8, 8, 8), jitter=0.02, seed=31)
-    e = _engine(mdgb, "mixed", trace=True)
+    e = _engine(mdgb, "mixed", trace=True, skin=0.3)   # a set skin: no tuning steps in the first call
     _upload(e, pos, vel, box)
     e.compute_forces()
     e.trace_phases()                      # reset
