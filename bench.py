@@ -100,6 +100,17 @@ def make_positions_oracle():
     return pos, box
 
 
+def fp64_pipe_fraction(atom_steps_per_s):
+    """The plain FP64 path against GB300's FP64 pipe: FP64 instructions per
+    atom-step (ncu, committed) x throughput / the measured DFMA rate."""
+    r = fp64_rates()
+    if not r:
+        return {}
+    achieved = r["fp64_pipe_thread_inst_per_atom_step"] * atom_steps_per_s
+    return {"fp64_pipe": {"bound": "fp64 pipe", "achieved_inst_per_s": achieved, "peak_dfma_per_s": r["dfma_per_s"],
+                          "frac": achieved / r["dfma_per_s"], "source": r["source"]}}
+
+
 def timing_note(st, steps):
     """How the timed steps ran, from the engine's own counters."""
     if st.graph_launches:
@@ -177,6 +188,16 @@ def measured_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def fp64_rates():
+    """FP64-pipe instructions per atom-step of the plain path's force pass and
+    the measured DFMA rate (profiles/fp64_rates.json), or None."""
+    p = os.path.join(ROOT, "profiles", "fp64_rates.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
 
 
 def ncu_traffic_per_atom():
@@ -466,8 +487,8 @@ def run_ours(args):
                                        "ms_per_step": t_prof / args.steps,
                                        "note": "per-launch CUDA events; gives the force-kernel time of the roofline"},
                        parallelism="replicas" if world > 1 else "single GPU",
-                       fp64_plain_path={"value": fp64_value, "unit": "atom-steps/s", "steps": k64,
-                                        "threads_per_atom": fp64_tpa},
+                       fp64_plain_path=dict({"value": fp64_value, "unit": "atom-steps/s", "steps": k64,
+                                             "threads_per_atom": fp64_tpa}, **fp64_pipe_fraction(fp64_value)),
                        mixed_over_fp64=value / fp64_value,
                        macro_err_vs_fp64=macro_err,
                        force_err_vs_fp64_oracle={"mixed": err_mixed, "fp64_plain": err_fp64,
@@ -567,7 +588,10 @@ def run_argon(args):
 def run_lj8m(args):
     """8,000,000 atoms: FCC 100x100x200 cells at rho* 0.8442, T* 0.72, Berendsen
     thermostat tau* 0.5 -> T* 0.72 and barostat (beta 1, tau_P* 5) -> P* 1.0,
-    500 steps; per-kernel roofline."""
+    500 steps; per-kernel roofline.  The timed leg records per-launch events
+    (force launches; step kernel + list-build kernel); a second run of the
+    same steps with the step kernel's phase trace splits the step kernel from
+    the list build."""
     global CELLS
     if not args.cells:
         CELLS = (100, 100, 200)
@@ -576,30 +600,41 @@ def run_lj8m(args):
     pos, vel, box = make_system(seed=88)
     n = len(pos)
     T0 = T_STAR * 100.0 / K_B
-    e = Engine(precision="mixed", skin=SKIN, profile=not args.trace, trace=args.trace)
-    e.set_potential(0, 0, 1.0, 1.0)
-    e.upload(np.zeros(n, dtype=np.uint16), pos, vel, [1.0], box)
-    e.compute_forces()
-    th, ba = Thermostat.Berendsen(0.5), Barostat.Berendsen(1.0, 5.0)
-    kw = dict(thermostat=th, target_temperature=T0, barostat=ba, target_pressure=1.0)
-    e.step(args.warmup, DT, **kw)
-    e.reset_stats()
-    if args.trace:
-        e.trace_phases()
-    with ClockSampler(0) as clk:
-        ms = _timed_steps(e, args.steps, DT, **kw)
-    st = e.stats()
-    phases = e.trace_phases() if args.trace else None
-    mac = e.macro(0)
-    end = e.download()
-    e.close()
+
+    def leg(trace):
+        e = Engine(precision="mixed", skin=SKIN, profile=not trace, trace=trace)
+        e.set_potential(0, 0, 1.0, 1.0)
+        e.upload(np.zeros(n, dtype=np.uint16), pos, vel, [1.0], box)
+        e.compute_forces()
+        th, ba = Thermostat.Berendsen(0.5), Barostat.Berendsen(1.0, 5.0)
+        kw = dict(thermostat=th, target_temperature=T0, barostat=ba, target_pressure=1.0)
+        e.step(args.warmup, DT, **kw)
+        e.reset_stats()
+        if trace:
+            e.trace_phases()
+        with ClockSampler(0) as clk:
+            ms = _timed_steps(e, args.steps, DT, **kw)
+        st = e.stats()
+        phases = e.trace_phases() if trace else None
+        mac = e.macro(0)
+        end = e.download()
+        e.close()
+        return ms, st, phases, mac, end, clk.summary()
+
+    ms, st, _, mac, end, clocks = leg(False)
+    _, st_t, phases, _, _, _ = leg(True)
     peak, kind = measured_peaks()
     f_ms = st.force_ms / max(st.force_launches, 1)
     p_ms = st.integrate_ms / max(st.integrate_launches, 1)
+    # the step kernel alone (its phases), per step; the list build per rebuild
+    steps_t = max(phases["launches"], 1.0)
+    pre_us = sum(v for k, v in phases.items() if k not in ("verlet_list", "launches", "rebuild_launches"))
+    list_us = phases["verlet_list"]
     # k_pre algorithmic bytes per atom without a rebuild: pos r/w 64, vel r/w 48,
-    # force read 24, cell 4, mirror write 16, mirror0 read 16, plus two FP64
-    # reduction passes over velocities and temp (2 x 32)
-    pre_bytes = 64 + 48 + 24 + 4 + 16 + 16 + 64
+    # force read 24, cell 4, mirror write 16, mirror0 read 16, plus the coupled
+    # steps' reduction pass over velocities, temp and potential (48)
+    pre_bytes = 64 + 48 + 24 + 4 + 16 + 16 + 48
+    pre_ms = pre_us / steps_t * 1e-3
     line = {"metric": METRIC, "value": n * args.steps / (ms * 1e-3), "unit": "atom-steps/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "dtype": "f32/i64-fixed/f64", "data": "synthetic: FCC 100x100x200, seeded T*=0.72",
@@ -607,16 +642,20 @@ def run_lj8m(args):
                        "atoms": n, "rebuilds": st.rebuilds,
                        "threads_per_atom": st.threads_per_atom, "final_T_star": mac["temperature"] * K_B / 100.0,
                        "final_P_star": mac["pressure"], "final_box": end["box"].tolist()},
-            "clocks": clk.summary(),
+            "clocks": clocks,
             "kernels": {"k_force_mixed": {"avg_ms": f_ms, "bytes_per_atom": BYTES_PER_ATOM_FORCE,
                                           "achieved_GBps": (BYTES_PER_ATOM_FORCE * n / (f_ms * 1e-3) / 1e9
                                                             if f_ms > 0 else None),
                                           "peak_GBps": peak, "peak_source": kind},
-                        "k_pre": {"avg_ms_incl_rebuilds": p_ms, "bytes_per_atom_no_rebuild": pre_bytes,
-                                  "achieved_GBps": pre_bytes * n / (p_ms * 1e-3) / 1e9 if p_ms > 0 else None,
-                                  "peak_GBps": peak}}}
-    if phases:
-        line["k_pre_phases_us"] = phases
+                        "k_pre": {"avg_ms": pre_ms, "source": "phase trace of the same steps (block 0 stamps)",
+                                  "bytes_per_atom_no_rebuild": pre_bytes,
+                                  "achieved_GBps": pre_bytes * n / (pre_ms * 1e-3) / 1e9 if pre_ms > 0 else None,
+                                  "peak_GBps": peak},
+                        "k_build_list": {"ms_per_rebuild": list_us / max(phases["rebuild_launches"], 1.0) * 1e-3,
+                                         "ms_per_step": list_us / steps_t * 1e-3},
+                        "k_pre_and_k_build_list_events_avg_ms": p_ms},
+            "k_pre_phases_us_per_step": {k: v / steps_t for k, v in phases.items()
+                                         if k not in ("launches", "rebuild_launches")}}
     print(json.dumps(line), flush=True)
 
 
@@ -666,7 +705,7 @@ def run_ensemble(args):
     res = {}
     # the mixed path with the skin chosen per size class by the engine, then
     # the same with the fixed 0.3 sigma skin, and the plain FP64 path
-    for leg, prec, skin in (("mixed", "mixed", 0.0), ("mixed_fixed_skin", "mixed", SKIN), ("fp64", "fp64", SKIN)):
+    for leg, prec, skin in (("mixed", "mixed", -1.0), ("mixed_fixed_skin", "mixed", SKIN), ("fp64", "fp64", SKIN)):
         e = Engine(precision=prec, skin=skin, persistent=True, graph_steps=50)
         e.set_potential(0, 0, 1.0, 1.0)
         e.upload_ensemble(offs, np.zeros(n, dtype=np.uint16), pos, vel, [1.0], boxes)
@@ -689,7 +728,7 @@ def run_ensemble(args):
                                                        ">=32768": st.class_threads_per_atom[2]},
                     "skin_sigma_by_size_class": {"<2048": st.class_skin[0], "2048-32767": st.class_skin[1],
                                                  ">=32768": st.class_skin[2]},
-                    "skin": "tuned per size class" if skin <= 0 else f"fixed {skin}",
+                    "skin": "tuned per size class" if skin < 0 else f"fixed {skin}",
                     "replicas_by_size_class": list(st.class_replicas)}
         e.close()
     if rank != 0:

@@ -103,9 +103,12 @@ typedef struct mdgb_engine mdgb_engine;
 
 typedef struct {
     int precision;          /* MDGB_PRECISION_* */
-    double skin;            /* Verlet skin (length); <= 0: chosen per replica size class on the first
-                               step call among 0.08 .. 0.16 x the largest r_cut (0.2 .. 0.4 sigma),
-                               by timing a short stretch of steps with each (state put back after) */
+    double skin;            /* Verlet skin (length); 0: 0.12 x the largest r_cut (0.3 sigma);
+                               < 0: chosen per replica size class on the first step call among
+                               0.08 .. 0.16 x the largest r_cut (0.2 .. 0.4 sigma) by timing a short
+                               stretch of steps with each (state put back after).  The choice follows
+                               the timings, so a tuned mixed-path run is not reproducible bit for bit
+                               across runs; an untuned one is. */
     int rebuild_every;      /* 0: rebuild when displacement needs it; >0: fixed interval, checked */
     int threads_per_atom;   /* 0: autotune; else 1, 2, 4 or 8 */
     int graph_steps;        /* >1: capture that many steps into one CUDA graph launch */
@@ -162,7 +165,7 @@ typedef struct {
     int64_t integrate_launches;
     int class_threads_per_atom[3]; /* autotuned per replica size class: <2048, <32768, larger */
     int class_replicas[3];
-    double class_skin[3];       /* Verlet skin per size class (tuned when mdgb_config.skin <= 0) */
+    double class_skin[3];       /* Verlet skin per size class (tuned when mdgb_config.skin < 0) */
 } mdgb_stats;
 
 /* ---- lifecycle ------------------------------------------------------- */

@@ -68,6 +68,11 @@ struct mdgb_engine {
     std::string err;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // the force launches of the size classes after the first run on their own
+    // streams, forked from and joined back into `stream` (also inside graphs)
+    cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[3] = {nullptr, nullptr, nullptr};
     int num_sms = 0;
     int pre_blocks_per_sm = 0;
     int force_blocks_per_sm[4] = {0, 0, 0, 0};
@@ -208,10 +213,13 @@ const LJ& pot_of(const mdgb_engine* e, int a, int b) {
 // Skin of size class c: the tuned one, else the configured (or default) one.
 double class_skin_of(const mdgb_engine* e, int c) { return e->skin_tuned ? e->class_skin[c] : e->skin; }
 
-// The configuration leaves the skin to the engine (reference-order runs keep
-// the default: their sums do not depend on the list).
+// The configuration asks the engine to choose the skin (skin < 0; 0 means
+// the default skin).  The choice comes from timings, and on the mixed path
+// the cell grid it implies changes FP32 roundings, so tuning is opt-in: an
+// untuned run is reproducible bit for bit.  Reference-order runs keep the
+// default (their sums do not depend on the list).
 bool skin_auto(const mdgb_engine* e) {
-    return !(e->cfg.skin > 0.0) && !((e->cfg.flags & MDGB_FLAG_REFERENCE_ORDER) && e->cfg.precision == MDGB_PRECISION_FP64);
+    return e->cfg.skin < 0.0 && !((e->cfg.flags & MDGB_FLAG_REFERENCE_ORDER) && e->cfg.precision == MDGB_PRECISION_FP64);
 }
 
 // Skin candidates of the tuning, as fractions of the largest r_cut
@@ -367,7 +375,7 @@ int force_grid(mdgb_engine* e, int c, bool kick) {
 
 // One force launch per non-empty size class, each with that class's threads
 // per atom (the replicas of a class were listed with the same layout).
-int launch_force_class(mdgb_engine* e, const StepParams& sp, bool kick, int c) {
+int launch_force_class(mdgb_engine* e, const StepParams& sp, bool kick, int c, cudaStream_t st) {
     const bool persistent = (e->cfg.flags & MDGB_FLAG_PERSISTENT) != 0;
     const int tpa = e->class_tpa[c];
     force_fn fn = force_kernel(tpa, e->cfg.precision, e->dev.single_type != 0, kick, persistent,
@@ -381,7 +389,7 @@ int launch_force_class(mdgb_engine* e, const StepParams& sp, bool kick, int c) {
     d.list_class = c;
     const int grid = force_grid(e, c, kick);
     void* args[] = {(void*)&d, (void*)&sp};
-    CU(cudaLaunchKernel((const void*)fn, dim3(grid), dim3(TILE * tpa), args, 0, e->stream));
+    CU(cudaLaunchKernel((const void*)fn, dim3(grid), dim3(TILE * tpa), args, 0, st));
     e->st.kernel_launches++;
     return MDGB_OK;
 }
@@ -394,9 +402,22 @@ int launch_force(mdgb_engine* e, const StepParams& sp_in, bool kick) {
     const StepParams& sp = sp_in;
     band_fn bk = band_kernel(e->cfg.precision);
     if (bk) CU(cudaMemsetAsync(e->dev.band_count, 0, sizeof(int), e->stream));
+    // classes touch disjoint atoms, tiles and queue counters: the second and
+    // third run concurrently with the first on their own streams
+    bool first = true;
     for (int c = 0; c < mdgb_engine::NCLASS; ++c) {
         if (!e->class_ntiles[c]) continue;
-        int rc = launch_force_class(e, sp, kick, c);
+        int rc;
+        if (first) {
+            CU(cudaEventRecord(e->fork_ev, e->stream));
+            rc = launch_force_class(e, sp, kick, c, e->stream);
+            first = false;
+        } else {
+            CU(cudaStreamWaitEvent(e->aux[c], e->fork_ev, 0));
+            rc = launch_force_class(e, sp, kick, c, e->aux[c]);
+            if (!rc) CU(cudaEventRecord(e->join_ev[c], e->aux[c]));
+            if (!rc) CU(cudaStreamWaitEvent(e->stream, e->join_ev[c], 0));
+        }
         if (rc) return rc;
     }
     if (bk) {
@@ -923,7 +944,7 @@ int autotune_tpa(mdgb_engine* e) {
         for (int c = 0; c < NC && !rc; ++c) {
             if (!e->class_ntiles[c]) continue;
             CU(cudaEventRecord(ev[c][0], e->stream));
-            for (int i = 0; i < 3 && !rc; ++i) rc = launch_force_class(e, sp, false, c);
+            for (int i = 0; i < 3 && !rc; ++i) rc = launch_force_class(e, sp, false, c, e->stream);
             CU(cudaEventRecord(ev[c][1], e->stream));
         }
         if (rc) break;
@@ -1143,6 +1164,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
             (rc = dalloc(e, &d.nn, N)) || (rc = dalloc(e, &d.tiles, ntiles)) ||
             (rc = dalloc(e, &d.rep, nrep)) || (rc = dalloc(e, &d.part, 8 * (size_t)ntiles)) ||
             (rc = dalloc(e, &d.cpart, 8 * chunks.size())) || (rc = dalloc(e, &d.chunks, chunks.size())) ||
+            (rc = dalloc(e, &d.fx_part, ntiles)) || (rc = dalloc(e, &d.fx_cpart, chunks.size())) ||
             (rc = dalloc(e, &d.err, 2)) || (rc = dalloc(e, &d.max_needed, 1)) ||
             (rc = dalloc(e, &d.cell_count, ncells)) ||
             (rc = dalloc(e, &d.cell_start, ncells + 1)) || (rc = dalloc(e, &d.cell_rep, ncells)) ||
@@ -1350,6 +1372,11 @@ mdgb_engine::~mdgb_engine() {
     for (auto& p : prof) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto& p : prof_free) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     if (h_err) cudaFreeHost(h_err);
+    for (int c = 0; c < 3; ++c) {
+        if (aux[c]) cudaStreamDestroy(aux[c]);
+        if (join_ev[c]) cudaEventDestroy(join_ev[c]);
+    }
+    if (fork_ev) cudaEventDestroy(fork_ev);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -1399,6 +1426,13 @@ MDGB_API int mdgb_create(const mdgb_config* cfg, mdgb_engine** out) {
     if (!prop.cooperativeLaunch) { delete e; return MDGB_ERR_UNSUPPORTED; }
     e->num_sms = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) { delete e; return MDGB_ERR_CUDA; }
+    for (int c = 0; c < mdgb_engine::NCLASS; ++c)
+        if (cudaStreamCreateWithFlags(&e->aux[c], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&e->join_ev[c], cudaEventDisableTiming) != cudaSuccess) {
+            delete e;
+            return MDGB_ERR_CUDA;
+        }
+    if (cudaEventCreateWithFlags(&e->fork_ev, cudaEventDisableTiming) != cudaSuccess) { delete e; return MDGB_ERR_CUDA; }
     int bps = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)k_pre, TILE, 0);
     int bps2 = 0;

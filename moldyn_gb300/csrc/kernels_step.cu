@@ -422,6 +422,263 @@ __device__ void phase_finalize_single(const Dev& d, const StepParams& sp, int se
     }
 }
 
+// ---------------------------------------------------------------------------
+// Exact sums for the mixed path's coupled steps (replaces the FP64 tree of
+// passes partials1 / chunk sums there).  A double x = m 2^(e - 1075)
+// (m < 2^53) goes onto the binary grid of its tile, unit 2^(T - 1075 - FX_K)
+// with T the largest exponent of that quantity in the tile, as a 128-bit
+// integer; tiles, then chunks, then replicas are added exactly after
+// aligning to the larger grid (bits below 2^-96 of the largest value drop,
+// toward zero).  Integer work only -- GB300's FP64 pipe is narrow -- and the
+// sums do not depend on the order of the additions.  Headroom: a tile sum is
+// below 2^104, a chunk sum below 2^112, a replica of up to 2^27 atoms below
+// 2^124.
+__device__ __forceinline__ int fx_exp(double x) {
+    const int e = (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FFull);
+    return e ? e : 1;   // subnormals and zero: exponent 1 without the hidden bit
+}
+
+__device__ __forceinline__ __int128 fx_place(double x, int T) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FFull);
+    unsigned long long m = b & 0x000FFFFFFFFFFFFFull;
+    if (e) m |= 1ull << 52;
+    const int s = (e ? e : 1) - T + FX_K;
+    __int128 v = 0;
+    if (s >= 0) v = (__int128)m << s;          // s <= FX_K: below 2^97
+    else if (s > -64) v = (__int128)(m >> (-s));
+    return (b >> 63) ? -v : v;
+}
+
+// v on grid T moved to the coarser grid Tmax >= T, toward zero
+__device__ __forceinline__ __int128 fx_align(__int128 v, int T, int Tmax) {
+    const int d = Tmax - T;
+    if (d == 0) return v;
+    if (d >= 127) return 0;
+    return v < 0 ? -((-v) >> d) : (v >> d);
+}
+
+__device__ __forceinline__ __int128 fx_shfl_xor(__int128 v, int o) {
+    const long long lo = __shfl_xor_sync(0xffffffffu, (long long)(unsigned long long)v, o);
+    const long long hi = __shfl_xor_sync(0xffffffffu, (long long)(v >> 64), o);
+    return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | (unsigned long long)lo);
+}
+
+// x * 2^(T - 1075 - FX_K) rounded to the nearest double (ties to even)
+__device__ __forceinline__ double fx_to_double(__int128 v, int T) {
+    if (v == 0) return 0.0;
+    const bool neg = v < 0;
+    const unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+    const unsigned long long hi = (unsigned long long)(u >> 64), lo = (unsigned long long)u;
+    const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+    unsigned long long mant;
+    int sh = 0;
+    if (p <= 52) {
+        mant = lo;
+    } else {
+        sh = p - 52;
+        mant = (unsigned long long)(u >> sh);
+        const unsigned __int128 rem = u & ((((unsigned __int128)1) << sh) - 1);
+        const unsigned __int128 half = ((unsigned __int128)1) << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+        if (mant >> 53) { mant >>= 1; ++sh; }
+    }
+    const double r = ldexp((double)mant, sh + T - 1075 - FX_K);
+    return neg ? -r : r;
+}
+
+// Pass 1 of a coupled step on the mixed path: one exact row per tile, one
+// warp per tile (four atoms per lane, all their loads issued before any
+// arithmetic; no block-wide synchronisation), warps striding over the tiles.
+__device__ void phase_partials_fx(const Dev& d, int sel) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int N = d.ntot;
+    for (int t = gw; t < d.ntiles; t += nw) {
+        const int4 tl = d.tiles[t];
+        double vx[4], vy[4], vz[4], vir[4], pot[4];
+        bool in[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int a = lane + 32 * k;
+            in[k] = a < tl.z;
+            const int s = tl.y + (in[k] ? a : 0);
+            vx[k] = __ldcg(d.vel + s); vy[k] = __ldcg(d.vel + N + s); vz[k] = __ldcg(d.vel + 2 * N + s);
+            vir[k] = __ldcg(d.evir + s); pot[k] = __ldcg(d.epot + s);
+            if (!d.single_type && in[k])
+                in[k] = (int)__ldcg(reinterpret_cast<const long long*>(d.pos + s) + 3) == sel;
+        }
+        double v2[4];
+        int ex[FX_NQ];
+#pragma unroll
+        for (int q = 0; q < FX_NQ; ++q) ex[q] = 1;
+        int nonfinite = 0;
+        unsigned cnt = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (!in[k]) { vx[k] = vy[k] = vz[k] = vir[k] = pot[k] = 0.0; }
+            v2[k] = __fma_rn(vz[k], vz[k], __fma_rn(vy[k], vy[k], __dmul_rn(vx[k], vx[k])));
+            cnt += __popc(__ballot_sync(0xffffffffu, in[k]));
+            const int e[FX_NQ] = {fx_exp(vx[k]), fx_exp(vy[k]), fx_exp(vz[k]), fx_exp(vir[k]), fx_exp(v2[k]),
+                                  fx_exp(pot[k])};
+#pragma unroll
+            for (int q = 0; q < FX_NQ; ++q) {
+                nonfinite |= e[q] == 0x7FF;
+                ex[q] = max(ex[q], e[q]);
+            }
+        }
+        nonfinite = __reduce_or_sync(0xffffffffu, nonfinite);
+        FxRow* row = d.fx_part + t;
+#pragma unroll
+        for (int q = 0; q < FX_NQ; ++q) {
+            const int T = __reduce_max_sync(0xffffffffu, ex[q]);
+            __int128 v = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const double xk = q == 0 ? vx[k] : q == 1 ? vy[k] : q == 2 ? vz[k] : q == 3 ? vir[k]
+                                : q == 4 ? v2[k] : pot[k];
+                v += fx_place(xk, T);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += fx_shfl_xor(v, o);
+            if (lane == 0) { row->s[q] = v; row->ex[q] = (unsigned short)T; }
+        }
+        if (lane == 0) { row->count = cnt; row->nonfinite = nonfinite; }
+    }
+}
+
+// Rows [0, n) added exactly by one warp: lane l takes rows l, l + 32, ...
+// (each row read whole, 128 bytes, eight 16-byte loads) onto its own running
+// grid, widened when a row needs it; then the lanes' sums onto the warp's
+// grid.  The result, valid in every lane, is on the grid of the largest
+// exponent.  Deterministic: the same rows always go to the same lanes in the
+// same order.
+__device__ __forceinline__ FxRow fx_warp_sum(const FxRow* rows, int n, int first = -1, int stride = 32) {
+    const int lane = threadIdx.x & 31;
+    if (first < 0) first = lane;
+    int T[FX_NQ];
+    __int128 s[FX_NQ];
+#pragma unroll
+    for (int q = 0; q < FX_NQ; ++q) { T[q] = 1; s[q] = 0; }
+    long long cnt = 0;
+    int nf = 0;
+    for (int t = first; t < n; t += stride) {
+        const longlong2* p = reinterpret_cast<const longlong2*>(rows + t);
+        longlong2 w[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) w[k] = __ldcg(p + k);
+        // w[0..5]: s[0..5] (low, high 64 bits); w[6]: ex[0..5] and nonfinite; w[7].x: count
+        const unsigned long long e03 = (unsigned long long)w[6].x;
+        const unsigned long long e45 = (unsigned long long)w[6].y;
+        int re[FX_NQ];
+        re[0] = (int)(e03 & 0xFFFF); re[1] = (int)((e03 >> 16) & 0xFFFF);
+        re[2] = (int)((e03 >> 32) & 0xFFFF); re[3] = (int)(e03 >> 48);
+        re[4] = (int)(e45 & 0xFFFF); re[5] = (int)((e45 >> 16) & 0xFFFF);
+        nf |= (int)(e45 >> 32);
+        cnt += w[7].x;
+#pragma unroll
+        for (int q = 0; q < FX_NQ; ++q) {
+            const longlong2 h = w[q];   // s[q] occupies 16 bytes: lo, hi
+            const __int128 v = (__int128)(((unsigned __int128)(unsigned long long)h.y << 64) |
+                                          (unsigned long long)h.x);
+            if (re[q] > T[q]) { s[q] = fx_align(s[q], T[q], re[q]); T[q] = re[q]; }
+            s[q] += fx_align(v, re[q], T[q]);
+        }
+    }
+    FxRow out;
+#pragma unroll
+    for (int q = 0; q < FX_NQ; ++q) {
+        const int Tw = __reduce_max_sync(0xffffffffu, T[q]);
+        __int128 v = fx_align(s[q], T[q], Tw);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += fx_shfl_xor(v, o);
+        out.s[q] = v;
+        out.ex[q] = (unsigned short)Tw;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        nf |= __shfl_xor_sync(0xffffffffu, nf, o);
+    }
+    out.count = cnt;
+    out.nonfinite = nf;
+    return out;
+}
+
+// The same with a whole block (threads take rows tid, tid + blockDim, ...),
+// then the warps' sums combined in a fixed order.  Result valid in thread 0.
+__device__ __forceinline__ FxRow fx_block_sum(const FxRow* rows, int n) {
+    __shared__ FxRow sm_w[TILE / 32];   // k_pre and k_macro blocks have TILE threads
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    FxRow r = fx_warp_sum(rows, n, (int)threadIdx.x, (int)blockDim.x);
+    __syncthreads();   // a previous call's rows are read
+    if (lane == 0) sm_w[w] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < nw; ++i) {
+            const FxRow& o = sm_w[i];
+#pragma unroll
+            for (int q = 0; q < FX_NQ; ++q) {
+                const int T = max((int)r.ex[q], (int)o.ex[q]);
+                r.s[q] = fx_align(r.s[q], r.ex[q], T) + fx_align(o.s[q], o.ex[q], T);
+                r.ex[q] = (unsigned short)T;
+            }
+            r.count += o.count;
+            r.nonfinite |= o.nonfinite;
+        }
+    }
+    return r;
+}
+
+// One block per chunk of tile rows.
+__device__ void phase_chunk_sums_fx(const Dev& d) {
+    for (int c = blockIdx.x; c < d.nchunks; c += gridDim.x) {
+        const int4 ch = d.chunks[c];
+        const FxRow r = fx_block_sum(d.fx_part + ch.y, ch.z);
+        if (threadIdx.x == 0) d.fx_cpart[c] = r;
+    }
+}
+
+// Mixed path, coupled steps: the replica's exact sums as doubles, then what
+// phase_finalize2 does (box, T, P, coupling).  sum_i |v_i - vcm|^2 = sum
+// |v_i|^2 - n |vcm|^2 (as sum v_i = n vcm): one pass over the atoms.
+__device__ void phase_finalize_fx(const Dev& d, const StepParams& sp, int sel) {
+    const double m = d.mass[sel];
+    for (int r = blockIdx.x; r < d.nrep; r += gridDim.x) {   // one block per replica
+        const RepDev R = load_rep(d.rep + r);
+        const FxRow F = fx_block_sum(d.fx_cpart + R.chunk_begin, R.nchunks);
+        if (threadIdx.x == 0) {
+            double S[7];
+            const double nan = __longlong_as_double(0x7FF8000000000000ll);
+            S[0] = fx_to_double(F.s[0], F.ex[0]); S[1] = fx_to_double(F.s[1], F.ex[1]);
+            S[2] = fx_to_double(F.s[2], F.ex[2]); S[3] = (double)F.count;
+            S[4] = fx_to_double(F.s[3], F.ex[3]); S[5] = fx_to_double(F.s[4], F.ex[4]);
+            S[6] = fx_to_double(F.s[5], F.ex[5]);
+            if (F.nonfinite)
+                for (int k = 0; k < 7; ++k) if (k != 3) S[k] = nan;
+            RepDev* W = d.rep + r;
+            const double vc[3] = {S[0] / S[3], S[1] / S[3], S[2] / S[3]};
+            W->vcm[0] = vc[0]; W->vcm[1] = vc[1]; W->vcm[2] = vc[2];
+            W->mom[0] = S[0] * m; W->mom[1] = S[1] * m; W->mom[2] = S[2] * m;
+            W->msum = S[3] * m; W->virsum = S[4]; W->ke = 0.5 * (m * S[5]); W->pe = S[6] * 0.5;
+            W->count = F.count;
+            const double p1 = m * (S[5] - S[3] * (vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]));
+            const double th = 0.5 * p1;
+            double box[3] = {R.box[0], R.box[1], R.box[2]};
+            if (R.pending != 1.0) {
+                for (int k = 0; k < d.ntypes; ++k)
+                    for (int a = 0; a < 3; ++a) box[a] *= R.pending;
+                for (int a = 0; a < 3; ++a) { W->box[a] = box[a]; W->cs[a] = box[a] / (double)R.nc[a]; }
+            }
+            const double volume = box[0] * box[1] * box[2];
+            const double T = temperature_of(th, F.count);
+            const double P = (p1 + (-S[4]) * 0.5) / volume / 3.0;
+            W->thermal = th; W->T = T; W->P = P;
+            coupling_factors(W, R, T, P, sp.dt);
+        }
+    }
+}
+
 // thermostat.rs:59-65: psi += psi_dot(T') * dt/2 with T' the temperature
 // after the first kick, before the velocity scaling.
 __device__ __forceinline__ void nh_update_psi(RepDev* W, const RepDev& R, double T, double dt) {
@@ -1067,11 +1324,11 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
             phase_serial(d, sp, sel, true);
             if (grid_barrier(d)) return;
         } else if (d.mixed) {
-            phase_partials1(d, sel);
+            phase_partials_fx(d, sel);
             if (grid_barrier(d)) return;
-            phase_chunk_sums<7>(d);
+            phase_chunk_sums_fx(d);
             if (grid_barrier(d)) return;
-            phase_finalize_single(d, sp, sel);
+            phase_finalize_fx(d, sp, sel);
             if (grid_barrier(d)) return;
         } else {
             phase_partials1(d, sel);

@@ -91,6 +91,20 @@ struct RepDev {
     long long count;
 };
 
+// One row of the exact (128-bit fixed-point) sums of the mixed path's coupled
+// steps: per quantity (v_x, v_y, v_z, temp, v.v, potential) an integer sum on
+// the binary grid of its exponent ex (unit 2^(ex - 1075 - FX_K)), the atom
+// count and a flag for non-finite inputs.  128 bytes.
+constexpr int FX_NQ = 6;
+constexpr int FX_K = 44;
+struct __align__(16) FxRow {
+    __int128 s[FX_NQ];
+    unsigned short ex[FX_NQ];
+    int nonfinite;
+    long long count;
+};
+static_assert(sizeof(FxRow) == 128, "FxRow is 128 bytes");
+
 struct StepParams {
     double dt;
     double kick_c[MAX_TYPES];  // dt / (2 m_t), computed on the host as the reference does
@@ -156,6 +170,8 @@ struct Dev {
     float4* mir_next;           //   and mirrors (the other buffer of each pair)
     int2* band_list;            // mixed path: atoms (index, replica) left to k_force_band
     int* band_count;
+    FxRow* fx_part;             // [ntiles] exact tile sums (mixed path, coupled steps)
+    FxRow* fx_cpart;            // [nchunks] exact chunk sums
 };
 
 // k_pre phases recorded with MDGB_FLAG_TRACE (slot indices; TR_SORT stays 0,

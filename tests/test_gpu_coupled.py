@@ -346,7 +346,7 @@ def test_nose_hoover_two_types_vs_oracle(Engine, oracle, precision, ref, tol):
 # skin tuning
 
 def test_skin_tuning_leaves_no_trace(Engine):
-    """skin <= 0: the first step call times a short stretch of steps with each
+    """skin < 0: the first step call times a short stretch of steps with each
     candidate skin (0.08 .. 0.16 of r_cut) and puts the state back.  The run
     then equals, bit for bit, engines configured with the chosen skins (the
     same cell grids and lists) that start from the same forces -- those the
@@ -358,7 +358,7 @@ def test_skin_tuning_leaves_no_trace(Engine):
     vel = np.concatenate([s[1] for s in systems])
     boxes = np.array([s[2] for s in systems])
     types = np.zeros(len(pos), dtype=np.uint16)
-    a = Engine(precision="mixed", threads_per_atom=1)
+    a = Engine(precision="mixed", threads_per_atom=1, skin=-1.0)
     a.set_potential(0, 0, 1.0, 1.0)
     a.upload_ensemble(offs, types, pos, vel, [1.0], boxes)
     a.compute_forces()

@@ -596,7 +596,7 @@ def test_trace_phases_account_for_the_step_kernel(mdgb):
     """MDGB_FLAG_TRACE: per-phase device time of the step kernel; launch and
     rebuild counts match the steps taken and the rebuild statistics."""
     pos, vel, box = gs.fcc((8, 8, 8), jitter=0.02, seed=31)
-    e = _engine(mdgb, "mixed", trace=True, skin=0.3)   # a set skin: no tuning steps in the first call
+    e = _engine(mdgb, "mixed", trace=True)
     _upload(e, pos, vel, box)
     e.compute_forces()
     e.trace_phases()                      # reset
@@ -611,3 +611,20 @@ def test_trace_phases_account_for_the_step_kernel(mdgb):
         assert ph["verlet_list"] > 0.0 and ph["gather"] > 0.0
     assert e.trace_phases()["launches"] == 0  # read-and-reset
     e.close()
+
+
+def test_fp64_rate_probe(tmp_path):
+    """The DFMA throughput the FP64 path's pipe fraction is quoted against
+    (tests/cuda/dfma_rate.cu): a plausible rate for GB300's FP64 pipe."""
+    import os
+    import re
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "dfma_rate")
+    subprocess.check_call(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                           os.path.join(root, "tests", "cuda", "dfma_rate.cu"), "-o", exe])
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    per_clk = float(re.search(r"per SM per clk at \d+ MHz: ([0-9.]+)", out.stdout).group(1))
+    print(out.stdout.strip())
+    assert 0.5 < per_clk < 4.0 and "err=no error" in out.stdout
