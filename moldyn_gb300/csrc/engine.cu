@@ -404,12 +404,14 @@ int launch_force(mdgb_engine* e, const StepParams& sp_in, bool kick) {
     if (bk) CU(cudaMemsetAsync(e->dev.band_count, 0, sizeof(int), e->stream));
     // classes touch disjoint atoms, tiles and queue counters: the second and
     // third run concurrently with the first on their own streams
+    int nclasses = 0;
+    for (int c = 0; c < mdgb_engine::NCLASS; ++c) nclasses += e->class_ntiles[c] ? 1 : 0;
     bool first = true;
     for (int c = 0; c < mdgb_engine::NCLASS; ++c) {
         if (!e->class_ntiles[c]) continue;
         int rc;
         if (first) {
-            CU(cudaEventRecord(e->fork_ev, e->stream));
+            if (nclasses > 1) CU(cudaEventRecord(e->fork_ev, e->stream));
             rc = launch_force_class(e, sp, kick, c, e->stream);
             first = false;
         } else {

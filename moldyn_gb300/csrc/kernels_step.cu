@@ -1,9 +1,12 @@
 // kernels_step.cu -- the per-step O(N) work of the engine in one cooperative
 // persistent kernel (k_pre), plus the macro-parameter reduction kernel.
 //
-//   [coupling]  FP64 reductions -> Berendsen lambda / mu
+//   [coupling]  reductions -> Berendsen lambda / mu
 //               (solver/src/initializer/thermostat.rs:24-34, barostat.rs:21-31,
-//                solver/src/macro_parameters/{mod,energy,pressure,temperature}.rs)
+//                solver/src/macro_parameters/{mod,energy,pressure,temperature}.rs):
+//               exact 128-bit fixed-point sums on the mixed path (integer
+//               work, phase_partials_fx), FP64 trees (or the reference's
+//               serial order) on the FP64 path
 //   [drift]     v += F dt/2m, thermostat scale, pending barostat scale of x,
 //               x += v dt, periodic wrap, FP32 mirror, displacement
 //               (solver/src/solver/integrator.rs:30-47, core/src/particle.rs:120-141)
@@ -22,10 +25,12 @@
 //
 // Phases are separated by a bounded grid barrier (the kernel is launched
 // cooperatively, so every block is resident).  A barrier that waits longer
-// than ~2 s sets E_TIMEOUT and lets the block continue; every index derived
-// from scratch data is range-checked, so a failed barrier cannot turn into
-// an out-of-bounds access.  Data produced by another block inside the same
-// launch is read with ld.global.cg (L2), never from a possibly stale L1 line.
+// than ~2 s sets E_TIMEOUT and the launch ends: every block stops at its next
+// barrier at the latest, so no phase runs on the incomplete results of the
+// one before (and the engine puts the chunk's starting state back).  Every
+// index derived from scratch data is range-checked as well.  Data produced by
+// another block inside the same launch is read with ld.global.cg (L2), never
+// from a possibly stale L1 line.
 //
 // This file is compiled with -fmad=false: its FP64 arithmetic (kick, drift,
 // wrap, reductions, coupling factors) keeps the reference's unfused
@@ -433,6 +438,11 @@ __device__ void phase_finalize_single(const Dev& d, const StepParams& sp, int se
 // sums do not depend on the order of the additions.  Headroom: a tile sum is
 // below 2^104, a chunk sum below 2^112, a replica of up to 2^27 atoms below
 // 2^124.
+// Below this many atoms the coupled reductions are latency-bound and the
+// FP64 tree (fewer dependent steps) is faster; from here on the exact sums
+// (no FP64 pipe work) are.
+constexpr int FX_MIN_ATOMS = 65536;
+
 __device__ __forceinline__ int fx_exp(double x) {
     const int e = (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FFull);
     return e ? e : 1;   // subnormals and zero: exponent 1 without the hidden bit
@@ -1323,12 +1333,19 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
         if (d.refmode) {
             phase_serial(d, sp, sel, true);
             if (grid_barrier(d)) return;
-        } else if (d.mixed) {
+        } else if (d.mixed && d.ntot >= FX_MIN_ATOMS) {
             phase_partials_fx(d, sel);
             if (grid_barrier(d)) return;
             phase_chunk_sums_fx(d);
             if (grid_barrier(d)) return;
             phase_finalize_fx(d, sp, sel);
+            if (grid_barrier(d)) return;
+        } else if (d.mixed) {
+            phase_partials1(d, sel);
+            if (grid_barrier(d)) return;
+            phase_chunk_sums<7>(d);
+            if (grid_barrier(d)) return;
+            phase_finalize_single(d, sp, sel);
             if (grid_barrier(d)) return;
         } else {
             phase_partials1(d, sel);

@@ -25,6 +25,8 @@
 // pixel shades its winner and blends the box edges in front of it.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include <algorithm>
 #include <vector>
 
@@ -243,6 +245,21 @@ __global__ void k_splat_shade(SplatDev s, const float4* __restrict__ part, const
 
 }  // namespace
 
+// Device buffers and a stream per GPU, kept between frames: they grow to the
+// largest frame drawn and stay until the process exits.
+namespace {
+constexpr int SPLAT_MAX_DEVICES = 64;
+struct SplatBuffers {
+    void* part = nullptr;
+    void* depth = nullptr;
+    void* out = nullptr;
+    size_t part_bytes = 0, depth_bytes = 0, out_bytes = 0;
+    cudaStream_t st = nullptr;
+};
+SplatBuffers g_splat_buf[SPLAT_MAX_DEVICES];
+std::mutex g_splat_mu[SPLAT_MAX_DEVICES];
+}  // namespace
+
 extern "C" MDGB_API int mdgb_splat(const float* particles, int64_t n, const mdgb_splat_params* prm, int width,
                                    int height, float* out_rgba) {
     if (n < 0 || (n > 0 && !particles) || !prm || !out_rgba || width <= 0 || height <= 0 ||
@@ -273,30 +290,43 @@ extern "C" MDGB_API int mdgb_splat(const float* particles, int64_t n, const mdgb
     s.height = height;
 
     const size_t npix = (size_t)width * height;
-    float4* d_part = nullptr;
-    unsigned long long* d_depth = nullptr;
-    float4* d_out = nullptr;
-    cudaStream_t st = nullptr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= SPLAT_MAX_DEVICES) return MDGB_ERR_CUDA;
+    // the device's buffers and stream, kept between frames (a frame of the
+    // same or a smaller size allocates nothing); one frame at a time per device
+    std::lock_guard<std::mutex> lock(g_splat_mu[dev]);
+    SplatBuffers& B = g_splat_buf[dev];
     int rc = MDGB_OK;
     auto ok = [&](cudaError_t e) {
         if (e != cudaSuccess && rc == MDGB_OK) rc = MDGB_ERR_CUDA;
         return e == cudaSuccess;
     };
-    if (ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) &&
-        ok(cudaMalloc(&d_part, std::max<size_t>(1, (size_t)n) * 3 * sizeof(float4))) &&
-        ok(cudaMalloc(&d_depth, npix * sizeof(unsigned long long))) && ok(cudaMalloc(&d_out, npix * sizeof(float4))) &&
-        (n == 0 || ok(cudaMemcpyAsync(d_part, particles, (size_t)n * 3 * sizeof(float4), cudaMemcpyHostToDevice, st))) &&
-        ok(cudaMemsetAsync(d_depth, 0xff, npix * sizeof(unsigned long long), st))) {
-        if (n > 0) k_splat_depth<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(s, d_part, n, d_depth);
-        k_splat_shade<<<dim3((width + 127) / 128, height), 128, 0, st>>>(s, d_part, d_depth, d_out);
-        if (ok(cudaGetLastError()) &&
-            ok(cudaMemcpyAsync(out_rgba, d_out, npix * sizeof(float4), cudaMemcpyDeviceToHost, st)))
-            ok(cudaStreamSynchronize(st));
+    auto grow = [&](void** p, size_t* have, size_t want) {
+        if (*have >= want) return true;
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+        *have = 0;
+        if (!ok(cudaMalloc(p, want))) return false;
+        *have = want;
+        return true;
+    };
+    const size_t part_bytes = std::max<size_t>(1, (size_t)n) * 3 * sizeof(float4);
+    if ((B.st || ok(cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking))) &&
+        grow(&B.part, &B.part_bytes, part_bytes) && grow(&B.depth, &B.depth_bytes, npix * sizeof(unsigned long long)) &&
+        grow(&B.out, &B.out_bytes, npix * sizeof(float4))) {
+        cudaStream_t st = B.st;
+        float4* d_part = static_cast<float4*>(B.part);
+        unsigned long long* d_depth = static_cast<unsigned long long*>(B.depth);
+        float4* d_out = static_cast<float4*>(B.out);
+        if ((n == 0 || ok(cudaMemcpyAsync(d_part, particles, (size_t)n * 3 * sizeof(float4), cudaMemcpyHostToDevice, st))) &&
+            ok(cudaMemsetAsync(d_depth, 0xff, npix * sizeof(unsigned long long), st))) {
+            if (n > 0) k_splat_depth<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(s, d_part, n, d_depth);
+            k_splat_shade<<<dim3((width + 127) / 128, height), 128, 0, st>>>(s, d_part, d_depth, d_out);
+            if (ok(cudaGetLastError()) &&
+                ok(cudaMemcpyAsync(out_rgba, d_out, npix * sizeof(float4), cudaMemcpyDeviceToHost, st)))
+                ok(cudaStreamSynchronize(st));
+        }
     }
-    if (d_part) cudaFree(d_part);
-    if (d_depth) cudaFree(d_depth);
-    if (d_out) cudaFree(d_out);
-    if (st) cudaStreamDestroy(st);
     if (rc != MDGB_OK) cudaGetLastError();
     return rc;
 }

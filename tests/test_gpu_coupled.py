@@ -407,3 +407,55 @@ def test_macro_getters_share_one_reduction(Engine):
     eng.step(1, DT)
     assert mp.get_kinetic_energy(st, 0) == eng.macro(0)["kinetic_energy"]
     set_precision("fp64")
+
+
+# --------------------------------------------------------------------------
+# exact sums of the coupled reductions (mixed path, from 65,536 atoms)
+
+@pytest.mark.parametrize("layout", ["single", "ensemble"])
+def test_exact_coupled_sums_match_the_fp64_reductions(Engine, layout):
+    """From 65,536 atoms the mixed path's coupled step sums velocities, |v|^2,
+    temp and potential exactly in 128-bit fixed point.  Its first step's
+    lambda and mu must equal the Berendsen formulas (thermostat.rs:31-34,
+    barostat.rs:29-30) evaluated on the temperature and pressure of the FP64
+    macro-parameter reduction of the same state, to 1e-14 (the two sums
+    differ by FP64 rounding only; cbrt/sqrt are CUDA's against numpy's)."""
+    from moldyn_gb300.initializer import Barostat, Thermostat
+    if layout == "single":
+        systems = [gs.fcc((26, 26, 26), jitter=0.03, seed=131, t_star=1.1)]           # 70,304 atoms
+    else:
+        systems = [gs.fcc((20, 20, 20), jitter=0.03, seed=132, t_star=0.9),           # 32,000
+                   gs.fcc((16, 16, 20), jitter=0.03, seed=133, t_star=1.4),           # 20,480
+                   gs.fcc((15, 15, 15), rho=0.7, jitter=0.03, seed=134, t_star=1.2)]  # 13,500
+        systems.append(gs.fcc((6, 6, 6), jitter=0.03, seed=135, t_star=0.8))          # 864
+    offs = np.cumsum([0] + [len(s[0]) for s in systems])
+    assert offs[-1] >= 65536
+    pos = np.concatenate([s[0] for s in systems])
+    vel = np.concatenate([s[1] for s in systems]) + 0.01 * np.arange(len(offs) - 1).repeat(np.diff(offs))[:, None]
+    boxes = np.array([s[2] for s in systems])
+    e = Engine(precision="mixed")
+    e.set_potential(0, 0, 1.0, 1.0)
+    types = np.zeros(len(pos), dtype=np.uint16)
+    if layout == "single":
+        e.upload(types, pos, vel, [1.0], boxes[0])
+    else:
+        e.upload_ensemble(offs, types, pos, vel, [1.0], boxes)
+    e.compute_forces()
+    mac = e.macro(0)
+    macs = [mac] if layout == "single" else mac
+    T0s = [gs.t_ref(0.72 + 0.1 * r) for r in range(len(systems))]
+    P0s = [1.0 - 0.2 * r for r in range(len(systems))]
+    ths = [Thermostat.Berendsen(TAU_T) for _ in systems]
+    bas = [Barostat.Berendsen(BETA, TAU_P) for _ in systems]
+    if layout == "single":
+        e.step(1, DT, thermostat=ths[0], target_temperature=T0s[0], barostat=bas[0], target_pressure=P0s[0])
+    else:
+        e.ensemble_set_coupling(ths, T0s, bas, P0s)
+        e.ensemble_step(1, DT)
+        e.ensemble_get_coupling()
+    for r, m in enumerate(macs):
+        lam = np.sqrt(1.0 + DT / TAU_T * (T0s[r] / m["temperature"] - 1.0))
+        myu = np.cbrt(1.0 + DT * BETA / TAU_P * (m["pressure"] - P0s[r]))
+        assert abs(ths[r].lambda_ - lam) <= 1e-14, (r, ths[r].lambda_, lam)
+        assert abs(bas[r].myu - myu) <= 1e-14, (r, bas[r].myu, myu)
+    e.close()
