@@ -100,6 +100,31 @@ def make_positions_oracle():
     return pos, box
 
 
+def issue_roofline(n_atoms, launch_ms, clocks):
+    """The force kernel against the SMs' instruction issue rate (what bounds
+    it; HBM does not): warp instructions per atom of one fused launch (ncu,
+    committed) x atoms / launch time, against 4 schedulers x SMs x clock."""
+    p = os.path.join(ROOT, "profiles", "force_mixed_traffic.json")
+    if not os.path.exists(p) or not launch_ms:
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    per_atom = d.get("warp_instructions_per_atom")
+    if not per_atom:
+        return None
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    sms = 152
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    achieved = per_atom * n_atoms / (launch_ms * 1e-3)
+    peak = 4.0 * sms * mhz * 1e6
+    return {"achieved": achieved, "peak": peak, "unit": "warp instructions/s", "frac": achieved / peak,
+            "warp_instructions_per_atom": per_atom, "sm_mhz": mhz}
+
+
 def fp64_pipe_fraction(atom_steps_per_s):
     """The plain FP64 path against GB300's FP64 pipe: FP64 instructions per
     atom-step (ncu, committed) x throughput / the measured DFMA rate."""
@@ -503,7 +528,8 @@ def run_ours(args):
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "bytes_per_atom": bytes_per_atom, "fused_drift_share": fused_fraction(args.steps),
                      "avg_launch_ms": force_ms_avg,
-                     "traffic": (tpa_traffic * n if tpa_traffic else None)},
+                     "traffic": (tpa_traffic * n if tpa_traffic else None),
+                     "issue": issue_roofline(n, force_ms_avg, clocks)},
         "cpu_baseline": {"value": cpu_value, "unit": "atom-steps/s", "cores": nthreads, "kind": "port",
                          "sample": f"oracle all-pairs update_force, rows 0..{rows} of {n} "
                                    f"(extrapolated from {rows} rows)"},
