@@ -62,8 +62,8 @@ __device__ __forceinline__ double ref_distance(const double4_32a pi, const doubl
 // l = v - h * 2^23 (|l| <= 2^22, exact in FP32).  Both are rounded to integers
 // by the magic-number method: adding M = 1.5 * 2^23 to a float of magnitude
 // <= 2^22 lands in [2^23, 2^24], where the float's bit pattern is
-// bits(M) + rint(x).  The bit patterns are summed modulo 2^32 and the offset
-// count * bits(M) removed at the end, so
+// bits(M) + rint(x).  Each term's bit pattern minus bits(M) is summed modulo
+// 2^32 (one three-input add per word), so
 //     sum_k rint(v_k) = (sum h_k) * 2^23 + sum l_k
 // exactly, in any order, for |v| <= 2^44 (the kernel re-accumulates an atom
 // with exact conversions when one of its terms may be larger).
@@ -74,12 +74,10 @@ constexpr int FIX_FOLD = 256;                      // most terms per lane the wo
 struct FixAcc {
     unsigned hi, lo;
     __device__ __forceinline__ void init() { hi = lo = 0u; }
-    // n terms added: remove the n magic offsets.  With n <= FIX_FOLD the two
-    // 32-bit words cannot overflow (|h| <= 2^21, |l| <= 2^22 per term).
-    __device__ __forceinline__ long long total(int n) const {
-        const int h = (int)(hi - (unsigned)n * FIX_MAGIC_BITS);
-        const int l = (int)(lo - (unsigned)n * FIX_MAGIC_BITS);
-        return ((long long)h << 23) + (long long)l;
+    // With at most FIX_FOLD terms the two 32-bit words cannot overflow
+    // (|h| <= 2^21, |l| <= 2^22 per term).
+    __device__ __forceinline__ long long total() const {
+        return ((long long)(int)hi << 23) + (long long)(int)lo;
     }
 };
 
@@ -94,16 +92,16 @@ __device__ __forceinline__ void fix_add_xyz(FixAcc& ax, FixAcc& ay, FixAcc& az, 
     const f2_t a2 = add2(t2, M2);
     const f2_t l2 = sub2(t2, sub2(a2, M2));
     const f2_t b2 = fma2(l2, K2, M2);
-    ax.hi += (unsigned)a2;
-    ay.hi += (unsigned)(a2 >> 32);
-    ax.lo += (unsigned)b2;
-    ay.lo += (unsigned)(b2 >> 32);
+    ax.hi += (unsigned)a2 - FIX_MAGIC_BITS;
+    ay.hi += (unsigned)(a2 >> 32) - FIX_MAGIC_BITS;
+    ax.lo += (unsigned)b2 - FIX_MAGIC_BITS;
+    ay.lo += (unsigned)(b2 >> 32) - FIX_MAGIC_BITS;
     const float tz = dz * g;
     const float az_ = tz + FIX_MAGIC;
     const float lz = tz - (az_ - FIX_MAGIC);
     const float bz = fmaf(lz, 8388608.0f, FIX_MAGIC);
-    az.hi += __float_as_uint(az_);
-    az.lo += __float_as_uint(bz);
+    az.hi += __float_as_uint(az_) - FIX_MAGIC_BITS;
+    az.lo += __float_as_uint(bz) - FIX_MAGIC_BITS;
 }
 
 template <int TPA>
@@ -298,12 +296,10 @@ struct MixedAcc {
     FixAcc ax, ay, az;
     float fx, fy, fz;
     float pe, vr, gmax;
-    int n;
     __device__ __forceinline__ void init() {
         ax.init(); ay.init(); az.init();
         fx = fy = fz = 0.f;
         pe = vr = gmax = 0.f;
-        n = 0;
     }
     // fscale_t: the fixed-point scale divided by 2^23; gmax tracks |fs| * fscale_t
     __device__ __forceinline__ void add(f2_t dxy, float dz, float r2, float fs, float u, float fscale_t) {
@@ -318,7 +314,6 @@ struct MixedAcc {
         const float g = fs * fscale_t;
         gmax = fmaxf(gmax, fabsf(g));
         fix_add_xyz(ax, ay, az, dxy, dz, g);
-        ++n;
     }
     __device__ __forceinline__ void add(float dx, float dy, float dz, float r2, float fs, float u, float fscale_t) {
         add(f2(dx, dy), dz, r2, fs, u, fscale_t);
@@ -403,7 +398,7 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
         }
         MixedAcc<NAIVE, NOE> acc;
         acc.init();
-        int ty = 0;
+        int ty = 0, n_own = 0;
         bool deferred = false;   // an atom with a pair in the band goes to k_force_band whole
         if (act) {
             const float4 xi = d.mir[s];
@@ -411,6 +406,7 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
             PairF P0{};
             if (SINGLE) P0 = pairf(d.pair[ty * MAX_TYPES + ty]);
             const int n = d.nn[s];
+            n_own = n;
             if (!brute) {
                 // hot loop: FP32 and integer work only, two candidates in flight
                 bool band = false;
@@ -422,9 +418,11 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
                     const PairF P = SINGLE ? P0 : pairf(d.pair[ty * MAX_TYPES + type_of(xj)]);
                     const float dx = f2_lo(dxy), dy = f2_hi(dxy);
                     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    // within 1e-5 of r_cut^2: the atom is finished by k_force_band
-                    band |= (r2 >= P.rc2_lo) & (r2 <= P.rc2_hi);
-                    if (r2 >= P.rc2_lo) return;
+                    if (r2 >= P.rc2_lo) {
+                        // within 1e-5 of r_cut^2: the atom is finished by k_force_band
+                        band |= r2 <= P.rc2_hi;
+                        return;
+                    }
                     float fs, u;
                     lj_f32(P, r2, fs, u);
                     acc.add(dxy, dz, r2, fs, u, fscale_t);
@@ -476,8 +474,10 @@ __global__ void __launch_bounds__(TILE * TPA, ((NOE ? 9 : 8) / TPA) > 0 ? ((NOE 
             const int slot = atomicAdd(d.band_count, 1);
             d.band_list[slot] = make_int2(s, tl.x);
         }
-        long long sx = acc.ax.total(acc.n), sy = acc.ay.total(acc.n), sz = acc.az.total(acc.n);
-        if (!NAIVE && act && !deferred && (acc.gmax > split_limit || acc.n > FIX_FOLD)) {
+        long long sx = acc.ax.total(), sy = acc.ay.total(), sz = acc.az.total();
+        // terms this lane summed: at most its share of the list
+        const int nl = act && n_own > lane ? (n_own - lane + TPA - 1) / TPA : 0;
+        if (!NAIVE && act && !deferred && (acc.gmax > split_limit || nl > FIX_FOLD)) {
             // a term may exceed the exact range of the split, or the lane summed
             // more terms than the 32-bit words hold: redo this lane's terms with
             // exact float -> int64 conversions (very close pairs, huge lists)
