@@ -43,6 +43,7 @@ RHO = 0.8442
 T_STAR = 0.72
 DT = 0.005
 SKIN = 0.3
+LIST_KW = {}   # --direct-list: {"direct_list": True}
 # algorithmic HBM bytes per atom of one force launch (mixed path, full list,
 # no Newton-3): list 4 B x 77.6 candidates (4/3 pi 2.8^3 rho*), own mirror 16,
 # count 4, force write 24, potential + temp write 16, velocity read+write 48.
@@ -341,7 +342,7 @@ def run_ours(args):
         """K steps from the seeded start after W warm-up steps: device time
         (CUDA events on the engine's stream, max over ranks), stats, clocks,
         end state."""
-        eng = Engine(precision=leg_precision, skin=SKIN, device=local, **kw)
+        eng = Engine(precision=leg_precision, skin=SKIN, device=local, **LIST_KW, **kw)
         eng.set_potential(0, 0, 1.0, 1.0)
         eng.upload(types, pos, vel, [1.0], box)
         eng.compute_forces()
@@ -380,7 +381,7 @@ def run_ours(args):
         phases = None
         if args.trace:
             te = Engine(precision="mixed", skin=SKIN, trace=True, device=local,
-                        threads_per_atom=st.threads_per_atom)
+                        threads_per_atom=st.threads_per_atom, **LIST_KW)
             te.set_potential(0, 0, 1.0, 1.0)
             te.upload(types, end["pos"], end["vel"], [1.0], box)
             te.compute_forces()
@@ -402,7 +403,7 @@ def run_ours(args):
     # once (the second upload of an unchanged shape keeps the device
     # allocations and the captured graphs, as a user's loop would).
     eng = Engine(precision="mixed", skin=SKIN, threads_per_atom=st.threads_per_atom, device=local,
-                 graph_steps=max(args.graph_steps, 0))
+                 graph_steps=max(args.graph_steps, 0), **LIST_KW)
     eng.set_potential(0, 0, 1.0, 1.0)
     host_out = {}
     eng.upload(types, pos, vel, [1.0], box)
@@ -876,6 +877,8 @@ def main():
     ap.add_argument("--legs", default="all", choices=["all", "mixed"],
                     help="'mixed' runs only the timed mixed leg (for profiler captures)")
     ap.add_argument("--trace", action="store_true", help="with --legs mixed: per-phase times of the step kernel")
+    ap.add_argument("--direct-list", action="store_true",
+                    help="lj1m: the direct Verlet-list build (every cell against 27 cells) instead of the paired one")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="with --legs mixed: the path whose steps are timed (profiler captures)")
     ap.add_argument("--tpa", type=int, default=0, help="threads per atom of the lj1m mixed leg (0: autotune)")
@@ -888,6 +891,8 @@ def main():
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     global CELLS
+    if args.direct_list:
+        LIST_KW["direct_list"] = True
     if args.cells:
         CELLS = tuple(int(c) for c in args.cells.split(","))
     if args.impl == "reference":

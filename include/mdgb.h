@@ -98,6 +98,11 @@ extern "C" {
 #define MDGB_FLAG_PERSISTENT 4u
 /* Record per-phase device time of the step kernel (mdgb_trace_phases). */
 #define MDGB_FLAG_TRACE 8u
+/* Build every neighbour list directly (each cell tests all 27 neighbour
+ * cells) instead of testing each pair of neighbouring cells once; the lists
+ * are the same.  The engine does this by itself for a rebuild in which a cell
+ * holds more than 32 atoms. */
+#define MDGB_FLAG_DIRECT_LIST 16u
 
 typedef struct mdgb_engine mdgb_engine;
 
@@ -166,6 +171,7 @@ typedef struct {
     int class_threads_per_atom[3]; /* autotuned per replica size class: <2048, <32768, larger */
     int class_replicas[3];
     double class_skin[3];       /* Verlet skin per size class (tuned when mdgb_config.skin < 0) */
+    int64_t direct_list_builds; /* list builds that took the direct path (MDGB_FLAG_DIRECT_LIST) */
 } mdgb_stats;
 
 /* ---- lifecycle ------------------------------------------------------- */

@@ -30,6 +30,7 @@ FLAG_REFERENCE_ORDER = 1
 FLAG_PROFILE = 2
 FLAG_PERSISTENT = 4
 FLAG_TRACE = 8
+FLAG_DIRECT_LIST = 16
 TRACE_PHASES = ["coupling", "drift", "decide", "zero_cells", "bin", "scan_a", "scan_b", "scan_c", "scatter",
                 "sort_cells", "gather", "verlet_list", "launches", "rebuild_launches"]
 THERMOSTAT_BERENDSEN = 0
@@ -72,7 +73,7 @@ class CStats(C.Structure):
                 ("force_ms", C.c_double), ("force_launches", C.c_int64),
                 ("integrate_ms", C.c_double), ("integrate_launches", C.c_int64),
                 ("class_threads_per_atom", C.c_int * 3), ("class_replicas", C.c_int * 3),
-                ("class_skin", C.c_double * 3)]
+                ("class_skin", C.c_double * 3), ("direct_list_builds", C.c_int64)]
 
 
 class CSplatParams(C.Structure):

@@ -121,7 +121,7 @@ struct mdgb_engine {
     uint16_t* d_in_t = nullptr;  // [N] caller type ids
     int* h_err = nullptr;        // pinned
     unsigned long long* trace_buf = nullptr;  // per-phase ns of k_pre (MDGB_FLAG_TRACE)
-    int lb_grid = 1, lb_cap = -1, lb_ncells = -1;  // list-build launch shape for (cap, cells)
+    int lb_grid = 1, lm_grid = 1, lb_cap = -1, lb_ncells = -1;  // list-build launch shapes for (cap, cells)
     // the other position / mirror buffer of each pair (fused NVE drift)
     double4_32a* pos_alt = nullptr;
     float4* mir_alt = nullptr;
@@ -139,7 +139,7 @@ struct mdgb_engine {
         Dev dev;
         const void* pos_alt;
         const void* mir_alt;
-        int class_tpa[3], class_ntiles[3], class_tile_off[3], pad;
+        int class_tpa[3], class_ntiles[3], class_tile_off[3], lm_grid;
     };
     struct GraphEntry {
         GraphKey key;
@@ -351,12 +351,13 @@ int launch_pre(mdgb_engine* e, const StepParams& sp) {
     CU(cudaLaunchKernelEx(&lc, k_pre, e->dev, sp));
     if (e->lb_cap != e->dev.cap || e->lb_ncells != e->dev.ncells) {
         e->lb_grid = list_build_grid(e->dev, e->num_sms);
+        e->lm_grid = list_masks_grid(e->dev, e->num_sms);
         e->lb_cap = e->dev.cap;
         e->lb_ncells = e->dev.ncells;
     }
-    CU(launch_list_build(e->dev, e->lb_grid, e->stream));
+    CU(launch_list_build(e->dev, e->lb_grid, e->lm_grid, e->stream));
     prof_end(e, pe);
-    e->st.kernel_launches += 2;
+    e->st.kernel_launches += 3;
     return MDGB_OK;
 }
 
@@ -491,7 +492,8 @@ int read_err(mdgb_engine* e, int* flags) {
 
 int clear_err(mdgb_engine* e) {
     CU(cudaMemsetAsync(e->dev.err, 0, 2 * sizeof(int), e->stream));
-    CU(cudaMemsetAsync(e->dev.bar, 0, 4 * sizeof(unsigned int), e->stream));
+    // bar[5] (direct list builds) is a counter: kept
+    CU(cudaMemsetAsync(e->dev.bar, 0, 5 * sizeof(unsigned int), e->stream));
     return MDGB_OK;
 }
 
@@ -641,6 +643,7 @@ mdgb_engine::GraphKey graph_key(const mdgb_engine* e, const StepParams& sp, int 
     std::memset(&k, 0, sizeof(k));   // padding included: keys compare as bytes
     k.len = n;
     k.lb_grid = e->lb_grid;
+    k.lm_grid = e->lm_grid;
     k.flags = e->cfg.flags;
     k.precision = e->cfg.precision;
     k.sp = sp;
@@ -664,6 +667,7 @@ mdgb_engine::GraphEntry* chunk_graph(mdgb_engine* e, const StepParams& sp, int n
     // the list-build grid is part of the key: settle it before the lookup
     if (e->lb_cap != e->dev.cap || e->lb_ncells != e->dev.ncells) {
         e->lb_grid = list_build_grid(e->dev, e->num_sms);
+        e->lm_grid = list_masks_grid(e->dev, e->num_sms);
         e->lb_cap = e->dev.cap;
         e->lb_ncells = e->dev.ncells;
     }
@@ -1151,6 +1155,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     d.refmode = (e->cfg.flags & MDGB_FLAG_REFERENCE_ORDER) && e->cfg.precision == MDGB_PRECISION_FP64 ? 1 : 0;
     d.mixed = e->cfg.precision != MDGB_PRECISION_FP64 ? 1 : 0;
     d.single_type = ntypes == 1 ? 1 : 0;
+    d.direct_list = (e->cfg.flags & MDGB_FLAG_DIRECT_LIST) ? 1 : 0;
     d.last_type = ntypes - 1;
     for (int t = 0; t < MAX_TYPES; ++t) d.mass[t] = t < ntypes ? mass_per_type[t] : 1.0;
 
@@ -1173,7 +1178,8 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
             (rc = dalloc(e, &d.perm, N)) || (rc = dalloc(e, &d.tmp_pos, N)) ||
             (rc = dalloc(e, &d.tmp_d, 8 * (size_t)N)) || (rc = dalloc(e, &d.tmp_i, 4 * (size_t)N)) ||
             (rc = dalloc(e, &d.slot_of_rank, N)) || (rc = dalloc(e, &d.bsum, 4096)) ||
-            (rc = dalloc(e, &d.bar, 4)) || (rc = dalloc(e, &d.queue, NC)) ||
+            (rc = dalloc(e, &d.lmask, 27 * (size_t)N)) || (rc = dalloc(e, &d.nbs, 27 * (size_t)ncells)) ||
+            (rc = dalloc(e, &d.bar, 8)) || (rc = dalloc(e, &d.queue, NC)) ||
             (rc = dalloc(e, &e->trace_buf, TR_SLOTS)) ||
             (rc = dalloc(e, &d.tile_order, ntiles)) ||
             (rc = dalloc(e, &e->snap_pos, N)) || (rc = dalloc(e, &e->snap_d, 8 * (size_t)N)) ||
@@ -1228,7 +1234,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     CU(cudaMemsetAsync(e->trace_buf, 0, TR_SLOTS * sizeof(unsigned long long), e->stream));
     d.trace = (e->cfg.flags & MDGB_FLAG_TRACE) ? e->trace_buf : nullptr;
     CU(cudaMemsetAsync(d.err, 0, 2 * sizeof(int), e->stream));
-    CU(cudaMemsetAsync(d.bar, 0, 4 * sizeof(unsigned int), e->stream));
+    CU(cudaMemsetAsync(d.bar, 0, 8 * sizeof(unsigned int), e->stream));
     CU(cudaMemcpyAsync(d.rep, e->rep_host.data(), nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
     // the caller's arrays, straight to the device staging
     double* dpos = e->d_out;
@@ -1693,6 +1699,9 @@ MDGB_API int mdgb_get_stats(mdgb_engine* e, mdgb_stats* out) {
             e->st.rebuilds = nb;
             e->st.max_neighbors = mx;
         }
+        unsigned int direct = 0;
+        if (cudaMemcpy(&direct, e->dev.bar + 5, sizeof(direct), cudaMemcpyDeviceToHost) == cudaSuccess)
+            e->st.direct_list_builds = direct;
     }
     e->st.neighbor_capacity = e->cap;
     e->st.threads_per_atom = e->tpa;
@@ -1733,6 +1742,7 @@ MDGB_API int mdgb_reset_stats(mdgb_engine* e) {
             for (auto& R : reps) R.nrebuilds = 0;
             cudaMemcpy(e->dev.rep, reps.data(), e->nrep * sizeof(RepDev), cudaMemcpyHostToDevice);
         }
+        cudaMemset(e->dev.bar + 5, 0, sizeof(unsigned int));
     }
     return MDGB_OK;
 }

@@ -123,7 +123,7 @@ struct StepParams {
 // Everything a kernel needs, passed by value.
 struct Dev {
     int ntot, ntiles, nrep, ntypes, cap, tpa, ncells;
-    int refmode, mixed, single_type, last_type, pad_dev;
+    int refmode, mixed, single_type, last_type, direct_list;   // direct_list: MDGB_FLAG_DIRECT_LIST
     double mass[MAX_TYPES];
     double rlist, rcmax, skin;   // rlist: the largest list radius of any replica
     float fscale, inv_fscale_f;  // fixed-point scale 2^fscale_log2
@@ -160,7 +160,10 @@ struct Dev {
     int* tmp_i;        // [4][N]: orig, rank, cell, slot within the cell
     int* slot_of_rank;
     int* bsum;         // [grid] scan block sums
-    unsigned int* bar; // [4] grid barrier: count, generation, any_rebuild, pad
+    unsigned int* bar; // [8] grid barrier count, generation; any rebuild; list-build blocks done;
+                       //   a cell too crowded for the paired list build; direct builds so far
+    uint32_t* lmask;   // [27][N] paired list build: hit word of (shift code, atom)
+    uint32_t* nbs;     // [ncells][27] start of each neighbour cell, tagged with its shift code
     unsigned int* queue;  // persistent force kernel work counters (one per size class)
     int* tile_order;   // tiles grouped by size class, costliest first inside a class
     const int* tile_list;  // the tiles one force launch covers (a size class)
@@ -200,7 +203,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // follows every k_pre launch and closes the rebuild k_pre started.
 cudaError_t list_build_init();
 int list_build_grid(const Dev& d, int num_sms);
-cudaError_t launch_list_build(const Dev& d, int grid, cudaStream_t st);
+int list_masks_grid(const Dev& d, int num_sms);
+cudaError_t launch_list_build(const Dev& d, int grid, int mgrid, cudaStream_t st);
 
 __device__ __forceinline__ int type_of(double4_32a p) { return (int)__double_as_longlong(p.w); }
 __device__ __forceinline__ int type_of(float4 p) { return __float_as_int(p.w); }

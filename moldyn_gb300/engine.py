@@ -42,6 +42,7 @@ class Stats:
     class_threads_per_atom: tuple = (0, 0, 0)
     class_replicas: tuple = (0, 0, 0)
     class_skin: tuple = (0.0, 0.0, 0.0)
+    direct_list_builds: int = 0
     extra: dict = field(default_factory=dict)
 
 
@@ -60,12 +61,15 @@ class Engine:
     "fp32_naive" (the precision study's variant: force sums in plain FP32).
     reference_order: FP64 only -- reproduce the reference's summation order so
     forces and trajectories are bit-identical to its FP64 CPU results.
+    direct_list: build every neighbour list directly (each cell against all
+    27 neighbour cells) rather than testing each pair of cells once; the same
+    lists, for comparison.
     """
 
     def __init__(self, precision: str = "mixed", skin: float = 0.0, rebuild_every: int = 0,
                  threads_per_atom: int = 0, graph_steps: int = 0, neighbor_capacity: int = 0,
                  device: int = 0, reference_order: bool = False, profile: bool = False,
-                 persistent: bool = False, trace: bool = False):
+                 persistent: bool = False, trace: bool = False, direct_list: bool = False):
         L = load()
         cfg = _lib.Config()
         check(L.mdgb_config_default(C.byref(cfg)))
@@ -80,7 +84,8 @@ class Engine:
         cfg.flags = ((_lib.FLAG_REFERENCE_ORDER if reference_order else 0)
                      | (_lib.FLAG_PROFILE if profile else 0)
                      | (_lib.FLAG_PERSISTENT if persistent else 0)
-                     | (_lib.FLAG_TRACE if trace else 0))
+                     | (_lib.FLAG_TRACE if trace else 0)
+                     | (_lib.FLAG_DIRECT_LIST if direct_list else 0))
         h = C.c_void_p()
         st = L.mdgb_create(C.byref(cfg), C.byref(h))
         if st != _lib.MDGB_OK:
