@@ -468,15 +468,18 @@ __device__ __forceinline__ void list_expand(const Dev& d, uint32_t* lb_smem) {
             own = false;
         }
         __syncwarp();
+        // nz: the codes whose word has a hit
+        int tot = 0;
+        uint32_t nz = 0u;
 #pragma unroll 9
         for (int k = 0; k < 27; ++k) {
-            wm[k * 32 + lane] = own ? __ldcs(d.lmask + (size_t)k * N + s) : 0u;
+            const uint32_t w = own ? __ldcs(d.lmask + (size_t)k * N + s) : 0u;
+            wm[k * 32 + lane] = w;
             wb[k * 32 + lane] = own ? __ldg(d.nbs + (size_t)c * 27 + k) : 0u;
+            tot += __popc(w);
+            nz |= (w != 0u ? 1u : 0u) << k;
         }
         __syncwarp();
-        int tot = 0;
-#pragma unroll
-        for (int k = 0; k < 27; ++k) tot += __popc(wm[k * 32 + lane]);
         // entries written (the rest of an overflowing list is only counted)
         const int lim = min(tot, cap);
         int lmax = lim;
@@ -484,16 +487,17 @@ __device__ __forceinline__ void list_expand(const Dev& d, uint32_t* lb_smem) {
         for (int off = 16; off > 0; off >>= 1) lmax = max(lmax, __shfl_xor_sync(FULL, lmax, off));
         uint32_t* rowp = d.nbr + (size_t)cap * (size_t)rbeg + (size_t)(s - rbeg) * (size_t)tpa;
         const size_t rowstride = (size_t)rn * (size_t)tpa;
-        // the next entry: lowest set bit of the current word; an empty word
-        // moves on to the next code (t < lim <= tot: a set bit remains)
-        int k = -1;
+        // the next entry: lowest set bit of the current word; an exhausted
+        // word moves on to the next code with a hit, in one step (t < lim <=
+        // tot: a set bit remains)
         uint32_t m = 0u, b = 0u;
         if (tpa == 1) {
 #pragma unroll 2
             for (int t = 0; t < lmax; ++t) {
                 if (t < lim) {
-                    while (m == 0u) {
-                        ++k;
+                    if (m == 0u) {
+                        const int k = __ffs(nz) - 1;
+                        nz &= nz - 1u;
                         m = wm[k * 32 + lane];
                         b = wb[k * 32 + lane];
                     }
@@ -506,8 +510,9 @@ __device__ __forceinline__ void list_expand(const Dev& d, uint32_t* lb_smem) {
             int col = 0;
             for (int t = 0; t < lmax; ++t) {
                 if (t < lim) {
-                    while (m == 0u) {
-                        ++k;
+                    if (m == 0u) {
+                        const int k = __ffs(nz) - 1;
+                        nz &= nz - 1u;
                         m = wm[k * 32 + lane];
                         b = wb[k * 32 + lane];
                     }
