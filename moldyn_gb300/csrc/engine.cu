@@ -1114,18 +1114,23 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     }
     std::vector<int> order(ntiles);
     for (int i = 0; i < ntiles; ++i) order[i] = i;
-    std::vector<double> cost(ntiles);
-    for (int i = 0; i < ntiles; ++i) {
-        const RepDev& R = reps[tiles[i].x];
-        const double vol = R.box[0] * R.box[1] * R.box[2];
-        const double dens = R.n / vol;
-        cost[i] = tiles[i].z * std::min((double)R.n, 1.0 + dens * 4.0 / 3.0 * M_PI * std::pow(e->rlist, 3));
+    if (nrep > 1) {
+        // expected pair work of a tile: its atoms x the replica's neighbours per atom
+        const double sphere = 4.0 / 3.0 * M_PI * e->rlist * e->rlist * e->rlist;
+        std::vector<double> rep_cost(nrep);
+        for (int r = 0; r < nrep; ++r) {
+            const RepDev& R = reps[r];
+            const double dens = R.n / (R.box[0] * R.box[1] * R.box[2]);
+            rep_cost[r] = std::min((double)R.n, 1.0 + dens * sphere);
+        }
+        struct Key { int cls; double cost; int tile; };
+        std::vector<Key> key(ntiles);
+        for (int i = 0; i < ntiles; ++i) key[i] = {class_of[tiles[i].x], tiles[i].z * rep_cost[tiles[i].x], i};
+        std::stable_sort(key.begin(), key.end(), [](const Key& a, const Key& b) {
+            return a.cls != b.cls ? a.cls < b.cls : a.cost > b.cost;
+        });
+        for (int i = 0; i < ntiles; ++i) order[i] = key[i].tile;
     }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        const int ca = class_of[tiles[a].x], cb = class_of[tiles[b].x];
-        if (ca != cb) return ca < cb;
-        return cost[a] > cost[b];
-    });
 
     // keep the allocations when the shape is unchanged
     Dev& d = e->dev;
