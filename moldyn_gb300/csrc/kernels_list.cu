@@ -66,6 +66,55 @@ __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane) {
     return x;
 }
 
+// Two own atoms (paired coordinates) against one candidate: r^2 - rlist^2
+// for each, negative when the pair is listed.  The sign is exact: the chain
+// ends in one rounding of a value that is zero only when r^2 = rlist^2.
+__device__ __forceinline__ f2_t pair_r2m(f2_t jx2, f2_t jy2, f2_t jz2, float4 A, float2 Z, f2_t nrl2) {
+    const f2_t ex = sub2(jx2, f2(A.x, A.y)), ey = sub2(jy2, f2(A.z, A.w)), ez = sub2(jz2, f2(Z.x, Z.y));
+    return fma2(ez, ez, fma2(ey, ey, fma2(ex, ex, nrl2)));
+}
+
+// Hit bits of one candidate against the own atoms (bit i: own atom i).  One
+// type: the own atoms in descending order, each sign bit shifted in from the
+// bottom (one funnel shift per test).  Several types: the reference's t1 <=
+// t2 loop (potential.rs:171-172) also decides, separately for each side --
+// fwd: own atom i lists the candidate (type_j >= type_i); bwd: the candidate
+// lists own atom i (type_i >= type_j).
+template <bool SINGLE, bool BWD>
+__device__ __forceinline__ void own_hits(f2_t jx2, f2_t jy2, f2_t jz2, int tj, int cpc4, const float4* own_xy,
+                                         const float2* own_z, const int* own_t, f2_t nrl2, uint32_t& fwd,
+                                         uint32_t& bwd) {
+    fwd = 0u;
+    bwd = 0u;
+    if (SINGLE) {
+        for (int i = cpc4 - 4; i >= 0; i -= 4) {
+#pragma unroll
+            for (int u = 2; u >= 0; u -= 2) {
+                const f2_t h = pair_r2m(jx2, jy2, jz2, own_xy[(i + u) >> 1], own_z[(i + u) >> 1], nrl2);
+                fwd = __funnelshift_l((unsigned)(h >> 32), fwd, 1);   // own atom i + u + 1
+                fwd = __funnelshift_l((unsigned)h, fwd, 1);           // own atom i + u
+            }
+        }
+        bwd = fwd;
+    } else {
+        for (int i = 0; i < cpc4; i += 4) {
+            const uint32_t b0 = 1u << i;
+#pragma unroll
+            for (int u = 0; u < 4; u += 2) {
+                const f2_t h = pair_r2m(jx2, jy2, jz2, own_xy[(i + u) >> 1], own_z[(i + u) >> 1], nrl2);
+                const bool h0 = f2_lo(h) < 0.f, h1 = f2_hi(h) < 0.f;
+                const int t0 = own_t[i + u], t1 = own_t[i + u + 1];
+                if (h0 & (tj >= t0)) fwd |= b0 << u;
+                if (h1 & (tj >= t1)) fwd |= b0 << (u + 1);
+                if (BWD) {
+                    if (h0 & (t0 >= tj)) bwd |= b0 << u;
+                    if (h1 & (t1 >= tj)) bwd |= b0 << (u + 1);
+                }
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // The paired build's tests.  Shared memory per warp, in 32-bit words: the
 // forward stream (A itself, then codes 14..26, at most 32 atoms a cell), the
@@ -99,7 +148,7 @@ __global__ void __launch_bounds__(LM_WARPS * 32) k_list_masks(Dev d) {
         const RepDev* W = d.rep + r;
         if (!W->rebuild || W->mode != MODE_CELLS) continue;
         const float rl = (float)(W->rlist * (1.0 + 1e-5));
-        const float rl2 = rl * rl;
+        const f2_t nrl2 = f2(-(rl * rl), -(rl * rl));
         const int nc[3] = {W->nc[0], W->nc[1], W->nc[2]};
         const int base = W->cell_base;
         const int local = c - base;
@@ -182,34 +231,9 @@ __global__ void __launch_bounds__(LM_WARPS * 32) k_list_masks(Dev d) {
                 e_n = cand[((q + 1) << 5) + lane];
                 x_n = __ldg(d.mir + (e_n & IDX_MASK));
             }
-            // bit i of `fwd`: own atom i lists this candidate; of `bwd`: the
-            // candidate lists own atom i (the reference's t1 <= t2 loop,
-            // potential.rs:171-172, decides each side by its own type)
-            uint32_t fwd = 0u, bwd = 0u;
-            for (int i = 0; i < cpc4; i += 4) {
-                const uint32_t b0 = 1u << i;
-#pragma unroll
-                for (int u = 0; u < 4; u += 2) {
-                    const float4 A = own_xy[(i + u) >> 1];
-                    const float2 Z = own_z[(i + u) >> 1];
-                    const f2_t ex = sub2(jx2, f2(A.x, A.y)), ey = sub2(jy2, f2(A.z, A.w)),
-                               ez = sub2(jz2, f2(Z.x, Z.y));
-                    const f2_t r2 = fma2(ez, ez, fma2(ey, ey, mul2(ex, ex)));
-                    const bool h0 = f2_lo(r2) < rl2, h1 = f2_hi(r2) < rl2;
-                    if (SINGLE) {
-                        if (h0) fwd |= b0 << u;
-                        if (h1) fwd |= b0 << (u + 1);
-                    } else {
-                        const int t0 = own_t[i + u], t1 = own_t[i + u + 1];
-                        if (h0 & (tj >= t0)) fwd |= b0 << u;
-                        if (h1 & (tj >= t1)) fwd |= b0 << (u + 1);
-                        if (h0 & (t0 >= tj)) bwd |= b0 << u;
-                        if (h1 & (t1 >= tj)) bwd |= b0 << (u + 1);
-                    }
-                }
-            }
+            uint32_t fwd, bwd;
+            own_hits<SINGLE, true>(jx2, jy2, jz2, tj, cpc4, own_xy, own_z, own_t, nrl2, fwd, bwd);
             if (!valid) fwd = bwd = 0u;
-            if (SINGLE) bwd = fwd;
             // the forward cell's atom: its word for the opposite code
             const int code = (int)(e >> IDX_BITS);
             if (valid && code != CODE_ZERO) d.lmask[(size_t)(26 - code) * N + (e & IDX_MASK)] = bwd;
@@ -257,7 +281,7 @@ __device__ __forceinline__ void list_direct(const Dev& d, uint32_t* lb_smem) {
         const RepDev* W = d.rep + r;
         if (!W->rebuild || W->mode != MODE_CELLS) continue;
         const float rl = (float)(W->rlist * (1.0 + 1e-5));
-        const float rl2 = rl * rl;
+        const f2_t nrl2 = f2(-(rl * rl), -(rl * rl));
         const int nc[3] = {W->nc[0], W->nc[1], W->nc[2]};
         const int base = W->cell_base;
         const int local = c - base;
@@ -349,23 +373,9 @@ __device__ __forceinline__ void list_direct(const Dev& d, uint32_t* lb_smem) {
                         e_n = cand[((q + 1) << 5) + lane];
                         x_n = __ldg(d.mir + (e_n & IDX_MASK));
                     }
-                    // bit i of `mine`: own atom i and this lane's candidate are within rlist
-                    uint32_t mine = 0u;
-                    for (int i = 0; i < cpc4; i += 4) {
-                        const uint32_t b0 = 1u << i;
-#pragma unroll
-                        for (int u = 0; u < 4; u += 2) {
-                            // own atoms i+u and i+u+1 against this lane's candidate
-                            const float4 A = own_xy[(i + u) >> 1];
-                            const float2 Z = own_z[(i + u) >> 1];
-                            const f2_t ex = sub2(jx2, f2(A.x, A.y)), ey = sub2(jy2, f2(A.z, A.w)),
-                                       ez = sub2(jz2, f2(Z.x, Z.y));
-                            const f2_t r2 = fma2(ez, ez, fma2(ey, ey, mul2(ex, ex)));
-                            // the reference's t1 <= t2 loop (potential.rs:171-172)
-                            if ((f2_lo(r2) < rl2) & (SINGLE || tj >= own_t[i + u])) mine |= b0 << u;
-                            if ((f2_hi(r2) < rl2) & (SINGLE || tj >= own_t[i + u + 1])) mine |= b0 << (u + 1);
-                        }
-                    }
+                    // bit i of `mine`: own atom i lists this lane's candidate
+                    uint32_t mine, unused;
+                    own_hits<SINGLE, false>(jx2, jy2, jz2, tj, cpc4, own_xy, own_z, own_t, nrl2, mine, unused);
                     if (!valid) mine = 0u;
                     // 32x32 bit transpose across the warp: lane i gets bit k set when
                     // candidate k of the chunk hits own atom i
@@ -468,16 +478,18 @@ __device__ __forceinline__ void list_expand(const Dev& d, uint32_t* lb_smem) {
             own = false;
         }
         __syncwarp();
-        // nz: the codes whose word has a hit
+        // words kept bit-reversed (the next entry is then the leading one, a
+        // single instruction); nz: the codes whose word has a hit, code k at
+        // bit 31 - k
         int tot = 0;
         uint32_t nz = 0u;
 #pragma unroll 9
         for (int k = 0; k < 27; ++k) {
             const uint32_t w = own ? __ldcs(d.lmask + (size_t)k * N + s) : 0u;
-            wm[k * 32 + lane] = w;
+            wm[k * 32 + lane] = __brev(w);
             wb[k * 32 + lane] = own ? __ldg(d.nbs + (size_t)c * 27 + k) : 0u;
             tot += __popc(w);
-            nz |= (w != 0u ? 1u : 0u) << k;
+            nz |= (w != 0u ? 0x80000000u : 0u) >> k;
         }
         __syncwarp();
         // entries written (the rest of an overflowing list is only counted)
@@ -492,32 +504,34 @@ __device__ __forceinline__ void list_expand(const Dev& d, uint32_t* lb_smem) {
         // tot: a set bit remains)
         uint32_t m = 0u, b = 0u;
         if (tpa == 1) {
+            uint32_t* wp = rowp;
 #pragma unroll 2
             for (int t = 0; t < lmax; ++t) {
                 if (t < lim) {
                     if (m == 0u) {
-                        const int k = __ffs(nz) - 1;
-                        nz &= nz - 1u;
+                        const int k = __clz(nz);
+                        nz ^= 0x80000000u >> k;
                         m = wm[k * 32 + lane];
                         b = wb[k * 32 + lane];
                     }
-                    const int p = __ffs(m) - 1;
-                    m &= m - 1u;
-                    rowp[(size_t)t * rowstride] = b + (uint32_t)p;
+                    const int p = __clz(m);
+                    m ^= 0x80000000u >> p;
+                    *wp = b + (uint32_t)p;
                 }
+                wp += rowstride;
             }
         } else {
             int col = 0;
             for (int t = 0; t < lmax; ++t) {
                 if (t < lim) {
                     if (m == 0u) {
-                        const int k = __ffs(nz) - 1;
-                        nz &= nz - 1u;
+                        const int k = __clz(nz);
+                        nz ^= 0x80000000u >> k;
                         m = wm[k * 32 + lane];
                         b = wb[k * 32 + lane];
                     }
-                    const int p = __ffs(m) - 1;
-                    m &= m - 1u;
+                    const int p = __clz(m);
+                    m ^= 0x80000000u >> p;
                     rowp[col] = b + (uint32_t)p;
                     if (++col == tpa) { col = 0; rowp += rowstride; }
                 }
