@@ -733,7 +733,7 @@ def run_ensemble(args):
     # the mixed path with the skin chosen per size class by the engine, then
     # the same with the fixed 0.3 sigma skin, and the plain FP64 path
     for leg, prec, skin in (("mixed", "mixed", -1.0), ("mixed_fixed_skin", "mixed", SKIN), ("fp64", "fp64", SKIN)):
-        e = Engine(precision=prec, skin=skin, persistent=True, graph_steps=50)
+        e = Engine(precision=prec, skin=skin, persistent=True, graph_steps=50, **LIST_KW)
         e.set_potential(0, 0, 1.0, 1.0)
         e.upload_ensemble(offs, np.zeros(n, dtype=np.uint16), pos, vel, [1.0], boxes)
         e.compute_forces()
@@ -878,7 +878,7 @@ def main():
                     help="'mixed' runs only the timed mixed leg (for profiler captures)")
     ap.add_argument("--trace", action="store_true", help="with --legs mixed: per-phase times of the step kernel")
     ap.add_argument("--direct-list", action="store_true",
-                    help="lj1m: the direct Verlet-list build (every cell against 27 cells) instead of the paired one")
+                    help="lj1m and ensemble: the direct Verlet-list build (every cell against 27 cells) instead of the paired one")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="with --legs mixed: the path whose steps are timed (profiler captures)")
     ap.add_argument("--tpa", type=int, default=0, help="threads per atom of the lj1m mixed leg (0: autotune)")

@@ -1077,7 +1077,10 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
         }
         const double vol = boxes[3 * r] * boxes[3 * r + 1] * boxes[3 * r + 2];
         max_density = std::max(max_density, nr / vol);
-        const double capd = std::min(std::ceil(prod * 1.3) + 27.0, 2.0 * nr + 27.0);
+        // cell capacity: the grid at this box with room to grow (barostat), but
+        // no finer than ~8 atoms a cell -- a dilute replica gets larger
+        // cells, so its rebuild is not dominated by per-cell work
+        const double capd = std::min(std::ceil(prod * 1.3) + 27.0, nr / 8.0 + 27.0);
         R.cell_cap = (int)std::max(27.0, capd);
         R.cell_base = (int)cell_rep.size();
         cell_rep.insert(cell_rep.end(), R.cell_cap, r);
@@ -1184,6 +1187,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
             (rc = dalloc(e, &d.tmp_d, 8 * (size_t)N)) || (rc = dalloc(e, &d.tmp_i, 4 * (size_t)N)) ||
             (rc = dalloc(e, &d.slot_of_rank, N)) || (rc = dalloc(e, &d.bsum, 4096)) ||
             (rc = dalloc(e, &d.lmask, 27 * (size_t)N)) || (rc = dalloc(e, &d.nbs, 27 * (size_t)ncells)) ||
+            (rc = dalloc(e, &d.rb, 4 + 3 * (size_t)nrep)) ||
             (rc = dalloc(e, &d.bar, 8)) || (rc = dalloc(e, &d.queue, NC)) ||
             (rc = dalloc(e, &e->trace_buf, TR_SLOTS)) ||
             (rc = dalloc(e, &d.tile_order, ntiles)) ||
@@ -1240,6 +1244,7 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     d.trace = (e->cfg.flags & MDGB_FLAG_TRACE) ? e->trace_buf : nullptr;
     CU(cudaMemsetAsync(d.err, 0, 2 * sizeof(int), e->stream));
     CU(cudaMemsetAsync(d.bar, 0, 8 * sizeof(unsigned int), e->stream));
+    CU(cudaMemsetAsync(d.rb, 0, (4 + 3 * (size_t)nrep) * sizeof(int), e->stream));
     CU(cudaMemcpyAsync(d.rep, e->rep_host.data(), nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
     // the caller's arrays, straight to the device staging
     double* dpos = e->d_out;

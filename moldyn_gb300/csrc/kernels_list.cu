@@ -10,7 +10,8 @@
 // pairs inside rlist, which the force kernels decide exactly.  Two builds
 // produce it:
 //
-// Paired (cells of at most 32 atoms, the usual case).  k_list_masks: one
+// Paired (replicas of at least LIST_PAIRED_MIN_ATOMS atoms whose cells hold
+// at most 32 atoms, the usual case).  k_list_masks: one
 // warp per cell A tests A's atoms against the atoms of A and of its 13
 // forward neighbour cells (codes 14..26), so each pair of neighbouring cells
 // is tested once, from one side.  A candidate stream of those cells is
@@ -25,8 +26,10 @@
 // pass, so in the [k / tpa][atom][k % tpa] layout the stores of a pass are
 // contiguous.
 //
-// Direct (a cell of more than 32 atoms anywhere in the rebuild, or
-// MDGB_FLAG_DIRECT_LIST).  One warp per cell, 32 of the cell's atoms at a
+// Direct (smaller replicas, where the second pass costs more than the
+// halved tests save; every replica when a cell of more than 32 atoms is
+// anywhere in the rebuild, or with MDGB_FLAG_DIRECT_LIST).  One warp per
+// cell, 32 of the cell's atoms at a
 // time ("own" atoms, staged in shared memory), tests the stream of all 27
 // neighbour cells, collects per lane a mask over the own atoms, transposes it
 // and expands each own atom's masks into its list.
@@ -129,7 +132,7 @@ static_assert((LM_WIN + 32 * LM_MQ) % 4 == 0 && LM_WARP_WORDS % 4 == 0, "float4 
 constexpr int LM_CELL_MAX = 32;      // atoms a cell may hold for the paired build
 
 template <bool SINGLE>
-__global__ void __launch_bounds__(LM_WARPS * 32) k_list_masks(Dev d) {
+__global__ void __launch_bounds__(LM_WARPS * 32, 10) k_list_masks(Dev d) {
     if (*(volatile const unsigned int*)(d.bar + 2) == 0u) return;   // no rebuild this step
     if (chunk_failed(d) || d.direct_list) return;
     __shared__ __align__(16) uint32_t lm_smem[LM_WARPS * LM_WARP_WORDS];
@@ -143,10 +146,15 @@ __global__ void __launch_bounds__(LM_WARPS * 32) k_list_masks(Dev d) {
     int* own_t = reinterpret_cast<int*>(own_z + 16);
     float4* tab = reinterpret_cast<float4*>(own_t + 32);
     const int gw = blockIdx.x * LM_WARPS + wib, nw = gridDim.x * LM_WARPS;
-    for (int c = gw; c < d.ncells; c += nw) {
-        const int r = d.cell_rep[c];
+    // the cells of the rebuilding replicas the paired build takes (the step
+    // kernel's work list, from position rb[1] on)
+    const int m = d.rb[0], w0 = rb_cell_off(d)[d.rb[1]], nwork = rb_cell_off(d)[m];
+    for (int wi = w0 + gw; wi < nwork; wi += nw) {
+        const int i = rb_locate(rb_cell_off(d), m, wi);
+        const int r = rb_rep(d)[i];
         const RepDev* W = d.rep + r;
-        if (!W->rebuild || W->mode != MODE_CELLS) continue;
+        if (W->mode != MODE_CELLS) continue;
+        const int c = W->cell_base + wi - rb_cell_off(d)[i];
         const float rl = (float)(W->rlist * (1.0 + 1e-5));
         const f2_t nrl2 = f2(-(rl * rl), -(rl * rl));
         const int nc[3] = {W->nc[0], W->nc[1], W->nc[2]};
@@ -262,8 +270,9 @@ __global__ void __launch_bounds__(LM_WARPS * 32) k_list_masks(Dev d) {
 }
 
 // The direct build: every cell against the stream of its 27 neighbour cells.
+// all: every rebuilding replica (else those the paired build does not take).
 template <bool SINGLE>
-__device__ __forceinline__ void list_direct(const Dev& d, uint32_t* lb_smem) {
+__device__ __forceinline__ void list_direct(const Dev& d, uint32_t* lb_smem, bool all) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint32_t* cand = lb_smem + (size_t)wib * LB_WARP_WORDS;
@@ -276,10 +285,15 @@ __device__ __forceinline__ void list_direct(const Dev& d, uint32_t* lb_smem) {
     float4* tab = reinterpret_cast<float4*>(own_t + 32);
     const int cap = d.cap;
     const int gw = blockIdx.x * LB_WARPS + wib, nw = gridDim.x * LB_WARPS;
-    for (int c = gw; c < d.ncells; c += nw) {
-        const int r = d.cell_rep[c];
+    // the cells of the rebuilding replicas this build takes (the step
+    // kernel's work list: all, or those before position rb[1])
+    const int m = d.rb[0], nwork = rb_cell_off(d)[all ? m : d.rb[1]];
+    for (int wi = gw; wi < nwork; wi += nw) {
+        const int i = rb_locate(rb_cell_off(d), m, wi);
+        const int r = rb_rep(d)[i];
         const RepDev* W = d.rep + r;
-        if (!W->rebuild || W->mode != MODE_CELLS) continue;
+        if (W->mode != MODE_CELLS) continue;
+        const int c = W->cell_base + wi - rb_cell_off(d)[i];
         const float rl = (float)(W->rlist * (1.0 + 1e-5));
         const f2_t nrl2 = f2(-(rl * rl), -(rl * rl));
         const int nc[3] = {W->nc[0], W->nc[1], W->nc[2]};
@@ -462,12 +476,17 @@ __device__ __forceinline__ void list_expand(const Dev& d, uint32_t* lb_smem) {
     const int cap = d.cap;
     constexpr int GPT = TILE / 32;                            // warp groups per tile
     const int gw = blockIdx.x * LB_WARPS + wib, nw = gridDim.x * LB_WARPS;
-    for (int g = gw; g < d.ntiles * GPT; g += nw) {
-        const int4 tl = d.tiles[g / GPT];
+    // the tiles of the rebuilding replicas the paired build takes (the step
+    // kernel's work list, from position rb[1] on)
+    const int m = d.rb[0], g0 = rb_tile_off(d)[d.rb[1]] * GPT, nwork = rb_tile_off(d)[m] * GPT;
+    for (int g = g0 + gw; g < nwork; g += nw) {
+        const int i = rb_locate(rb_tile_off(d), m, g / GPT);
+        const int r = rb_rep(d)[i];
+        const RepDev* W = d.rep + r;
+        if (W->mode != MODE_CELLS) continue;
+        const int4 tl = d.tiles[W->tile_begin + g / GPT - rb_tile_off(d)[i]];
         const int sub = (g % GPT) * 32;
         if (sub >= tl.z) continue;
-        const RepDev* W = d.rep + tl.x;
-        if (!W->rebuild || W->mode != MODE_CELLS) continue;
         const long long rbeg = W->begin;
         const int rn = W->n, tpa = W->tpa;
         const int s = tl.y + sub + lane;
@@ -563,8 +582,8 @@ __global__ void __launch_bounds__(LB_WARPS * 32, 11) k_build_list(Dev d) {
     __shared__ int s_last;
     // the paired build's masks are complete unless a cell was too crowded for them
     const bool direct = d.direct_list || *(volatile const unsigned int*)(d.bar + 4) != 0u;
-    if (direct) list_direct<SINGLE>(d, lb_smem);
-    else list_expand(d, lb_smem);
+    list_direct<SINGLE>(d, lb_smem, direct);
+    if (!direct) list_expand(d, lb_smem);
     // The last block to finish closes the rebuild of every replica.
     __syncthreads();
     if (threadIdx.x == 0) {

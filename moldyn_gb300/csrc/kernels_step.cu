@@ -913,6 +913,71 @@ __device__ void phase_decide(const Dev& d, const StepParams& sp) {
 // ---------------------------------------------------------------------------
 // Rebuild phases (only tiles/cells of replicas with rebuild set do work).
 
+// The rebuild work list (block 0; the grid barrier after the zero phase
+// publishes it): the rebuilding replicas with prefix offsets of their cells
+// (the grid the decide phase set; one cell in brute mode) and tiles, so the
+// rebuild phases and the list build visit only their work.  Replicas the
+// paired list build does not take come first (pass 0), the others after.
+__device__ void phase_work_list(const Dev& d) {
+    __shared__ int wsum[3][TILE / 32];
+    __shared__ int carry[3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int* rb = d.rb;
+    int* ids = rb + 2;
+    int* coff = rb + 2 + d.nrep;
+    int* toff = rb + 3 + 2 * d.nrep;
+    if (threadIdx.x < 3) carry[threadIdx.x] = 0;
+    __syncthreads();
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int base = 0; base < d.nrep; base += blockDim.x) {
+            const int r = base + threadIdx.x;
+            int v[3] = {0, 0, 0};
+            if (r < d.nrep) {
+                const RepDev* W = d.rep + r;
+                const bool paired = W->n >= LIST_PAIRED_MIN_ATOMS && __ldcg(&W->mode) == MODE_CELLS;
+                if (__ldcg(&W->rebuild) && paired == (pass == 1)) {
+                    v[0] = 1;
+                    v[1] = __ldcg(&W->nc[0]) * __ldcg(&W->nc[1]) * __ldcg(&W->nc[2]);
+                    v[2] = W->ntiles;
+                }
+            }
+            int inc[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                inc[q] = v[q];
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, inc[q], off);
+                    if (lane >= off) inc[q] += y;
+                }
+                if (lane == 31) wsum[q][w] = inc[q];
+            }
+            __syncthreads();
+            if (v[0]) {
+                int ex[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    ex[q] = carry[q] + inc[q] - v[q];
+                    for (int k = 0; k < w; ++k) ex[q] += wsum[q][k];
+                }
+                ids[ex[0]] = r;
+                coff[ex[0]] = ex[1];
+                toff[ex[0]] = ex[2];
+            }
+            __syncthreads();
+            if (threadIdx.x < 3)
+                for (int k = 0; k < (int)(blockDim.x >> 5); ++k) carry[threadIdx.x] += wsum[threadIdx.x][k];
+            __syncthreads();
+        }
+        if (pass == 0 && threadIdx.x == 0) rb[1] = carry[0];
+    }
+    if (threadIdx.x == 0) {
+        rb[0] = carry[0];
+        coff[carry[0]] = carry[1];
+        toff[carry[0]] = carry[2];
+    }
+}
+
 __device__ void phase_zero_cells(const Dev& d) {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int nt = gridDim.x * blockDim.x;
@@ -928,10 +993,12 @@ __device__ void phase_zero_cells(const Dev& d) {
 __device__ void phase_bin(const Dev& d) {
     const int N = d.ntot;
     const int lane = threadIdx.x & 31;
-    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
-        const int4 tl = d.tiles[t];
+    const int m = __ldcg(d.rb), nw = __ldcg(rb_tile_off(d) + m);
+    for (int wi = blockIdx.x; wi < nw; wi += gridDim.x) {
+        const int i = rb_locate(rb_tile_off(d), m, wi);
+        const int r = __ldcg(rb_rep(d) + i);
+        const int4 tl = d.tiles[d.rep[r].tile_begin + wi - __ldcg(rb_tile_off(d) + i)];
         const RepDev& R = tile_rep(d, tl.x);
-        if (!R.rebuild) continue;
         const int s = tl.y + threadIdx.x;
         const bool act = (int)threadIdx.x < tl.z;
         const unsigned am = __ballot_sync(0xffffffffu, act);
@@ -1028,10 +1095,12 @@ __device__ void phase_scan_c(const Dev& d, int chunk) {
 // follows); a step's force pass rewrites them after the rebuild anyway.
 __device__ void phase_scatter(const Dev& d, bool carry_forces) {
     const int N = d.ntot;
-    for (int t = blockIdx.x; t < d.ntiles; t += gridDim.x) {
-        const int4 tl = d.tiles[t];
+    const int m = __ldcg(d.rb), nw = __ldcg(rb_tile_off(d) + m);
+    for (int wi = blockIdx.x; wi < nw; wi += gridDim.x) {
+        const int i = rb_locate(rb_tile_off(d), m, wi);
+        const int r = __ldcg(rb_rep(d) + i);
+        const int4 tl = d.tiles[d.rep[r].tile_begin + wi - __ldcg(rb_tile_off(d) + i)];
         const RepDev& R = tile_rep(d, tl.x);
-        if (!R.rebuild) continue;
         const int s = tl.y + threadIdx.x;
         if ((int)threadIdx.x >= tl.z) continue;
         const int cell = d.tmp_i[2 * (size_t)N + s];
@@ -1123,9 +1192,11 @@ __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
     const int nw = (gridDim.x * blockDim.x) >> 5;
     CellGeom g;
     g.r = -1;
-    for (int c = gw; c < d.ncells; c += nw) {
-        const int r = d.cell_rep[c];
-        if (!__ldcg(&d.rep[r].rebuild)) continue;
+    const int m = __ldcg(d.rb), nwork = __ldcg(rb_cell_off(d) + m);
+    for (int wi = gw; wi < nwork; wi += nw) {
+        const int i = rb_locate(rb_cell_off(d), m, wi);
+        const int r = __ldcg(rb_rep(d) + i);
+        const int c = __ldcg(&d.rep[r].cell_base) + wi - __ldcg(rb_cell_off(d) + i);
         const int b = __ldcg(d.cell_start + c), n = __ldcg(d.cell_count + c);
         if (n <= 0) continue;
         if (b < 0 || b + n > N) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
@@ -1144,13 +1215,18 @@ __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
                 key[q] = ok ? __ldcg(d.tmp_i + e[q]) : 0x7FFFFFFF;
                 rank[q] = 0;
             }
+            if (n <= 32) {
+                // the common case: one key a lane, n shuffles
+                for (int k = 0; k < n; ++k) rank[0] += (__shfl_sync(0xffffffffu, key[0], k) < key[0]) ? 1 : 0;
+            } else {
 #pragma unroll
-            for (int q2 = 0; q2 < SORT_MAX_PER_LANE; ++q2) {
-                if (q2 * 32 >= n) break;
-                for (int k = 0; k < 32; ++k) {
-                    const int kk = __shfl_sync(0xffffffffu, key[q2], k);
+                for (int q2 = 0; q2 < SORT_MAX_PER_LANE; ++q2) {
+                    if (q2 * 32 >= n) break;
+                    for (int k = 0; k < 32; ++k) {
+                        const int kk = __shfl_sync(0xffffffffu, key[q2], k);
 #pragma unroll
-                    for (int q = 0; q < SORT_MAX_PER_LANE; ++q) rank[q] += (kk < key[q]) ? 1 : 0;
+                        for (int q = 0; q < SORT_MAX_PER_LANE; ++q) rank[q] += (kk < key[q]) ? 1 : 0;
+                    }
                 }
             }
 #pragma unroll
@@ -1388,6 +1464,7 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
 
 // The rebuild phases of k_pre (replicas with their rebuild flag set).
 __device__ __forceinline__ void k_pre_rebuild(const Dev& d, const StepParams& sp, PhaseClock& clk) {
+    if (blockIdx.x == 0) phase_work_list(d);
     phase_zero_cells(d);
     if (grid_barrier(d)) return;
     clk.mark(TR_ZERO);

@@ -162,6 +162,11 @@ struct Dev {
     int* bsum;         // [grid] scan block sums
     unsigned int* bar; // [8] grid barrier count, generation; any rebuild; list-build blocks done;
                        //   a cell too crowded for the paired list build; direct builds so far
+    int* rb;           // rebuild work list, built by the step kernel when it rebuilds:
+                       //   [0] count m of rebuilding replicas, [1] how many of them come
+                       //   first because the paired list build does not take them (brute
+                       //   mode, or fewer than LIST_PAIRED_MIN_ATOMS atoms), then nrep ids,
+                       //   m + 1 prefix offsets of their cells and m + 1 of their tiles
     uint32_t* lmask;   // [27][N] paired list build: hit word of (shift code, atom)
     uint32_t* nbs;     // [ncells][27] start of each neighbour cell, tagged with its shift code
     unsigned int* queue;  // persistent force kernel work counters (one per size class)
@@ -197,6 +202,22 @@ __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
+}
+
+// The rebuild work list (Dev::rb): replica ids and prefix offsets of their
+// cells and tiles.  Work item w (a cell or a tile of a rebuilding replica,
+// counted over the list) -> the list position i with off[i] <= w < off[i+1].
+constexpr int LIST_PAIRED_MIN_ATOMS = 32768;  // smaller replicas: the direct list build
+__device__ __forceinline__ const int* rb_rep(const Dev& d) { return d.rb + 2; }
+__device__ __forceinline__ const int* rb_cell_off(const Dev& d) { return d.rb + 2 + d.nrep; }
+__device__ __forceinline__ const int* rb_tile_off(const Dev& d) { return d.rb + 3 + 2 * d.nrep; }
+__device__ __forceinline__ int rb_locate(const int* off, int m, int w) {
+    int lo = 0, hi = m - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldcg(off + mid) <= w) lo = mid; else hi = mid - 1;
+    }
+    return lo;
 }
 
 // Verlet-list build for cell-mode replicas (kernels_list.cu): a kernel that
