@@ -832,16 +832,20 @@ __device__ void phase_drift(const Dev& d, const StepParams& sp, bool kicked) {
     constexpr bool fm = FM;
     int tc_rep = -1;          // replica tc[] and disp belong to (block-uniform)
     float disp = 0.f;         // largest displacement seen by this thread in replica tc_rep
-    int t = blockIdx.x;
-    int4 tl = t < d.ntiles ? d.tiles[t] : make_int4(0, 0, 0, 0);
+    // a contiguous run of tiles per block: the replica (and with it the
+    // constants and the displacement maximum) changes only at its boundaries
+    const int per = (d.ntiles + gridDim.x - 1) / gridDim.x;
+    const int t_end = min(d.ntiles, ((int)blockIdx.x + 1) * per);
+    int t = blockIdx.x * per;
+    int4 tl = t < t_end ? d.tiles[t] : make_int4(0, 0, 0, 0);
     DriftIn cur;
-    if (t < d.ntiles && (int)threadIdx.x < tl.z) drift_load(d, tl.y + threadIdx.x, kicked, cur);
-    for (; t < d.ntiles; t += gridDim.x) {
+    if (t < t_end && (int)threadIdx.x < tl.z) drift_load(d, tl.y + threadIdx.x, kicked, cur);
+    for (; t < t_end; ++t) {
         // the next tile's inputs in flight while this one computes
-        const int tn = t + gridDim.x;
+        const int tn = t + 1;
         int4 tln = make_int4(0, 0, 0, 0);
         DriftIn nxt;
-        if (tn < d.ntiles) {
+        if (tn < t_end) {
             tln = d.tiles[tn];
             if ((int)threadIdx.x < tln.z) drift_load(d, tln.y + threadIdx.x, kicked, nxt);
         }
@@ -993,11 +997,21 @@ __device__ void phase_zero_cells(const Dev& d) {
 __device__ void phase_bin(const Dev& d) {
     const int N = d.ntot;
     const int lane = threadIdx.x & 31;
+    // a contiguous run of the rebuilding replicas' tiles per block (the
+    // replica record is fetched only when the run crosses into the next)
     const int m = __ldcg(d.rb), nw = __ldcg(rb_tile_off(d) + m);
-    for (int wi = blockIdx.x; wi < nw; wi += gridDim.x) {
-        const int i = rb_locate(rb_tile_off(d), m, wi);
-        const int r = __ldcg(rb_rep(d) + i);
-        const int4 tl = d.tiles[d.rep[r].tile_begin + wi - __ldcg(rb_tile_off(d) + i)];
+    const int per = (nw + gridDim.x - 1) / gridDim.x;
+    const int w_end = min(nw, ((int)blockIdx.x + 1) * per);
+    int wi = blockIdx.x * per;
+    int i = wi < w_end ? rb_locate(rb_tile_off(d), m, wi) - 1 : 0;
+    int next = wi, shift = 0;   // where replica i's run ends; tile index - work index inside it
+    for (; wi < w_end; ++wi) {
+        while (wi >= next) {
+            ++i;
+            next = __ldcg(rb_tile_off(d) + i + 1);
+            shift = d.rep[__ldcg(rb_rep(d) + i)].tile_begin - __ldcg(rb_tile_off(d) + i);
+        }
+        const int4 tl = d.tiles[wi + shift];
         const RepDev& R = tile_rep(d, tl.x);
         const int s = tl.y + threadIdx.x;
         const bool act = (int)threadIdx.x < tl.z;
@@ -1095,11 +1109,21 @@ __device__ void phase_scan_c(const Dev& d, int chunk) {
 // follows); a step's force pass rewrites them after the rebuild anyway.
 __device__ void phase_scatter(const Dev& d, bool carry_forces) {
     const int N = d.ntot;
+    // a contiguous run of the rebuilding replicas' tiles per block (the
+    // replica record is fetched only when the run crosses into the next)
     const int m = __ldcg(d.rb), nw = __ldcg(rb_tile_off(d) + m);
-    for (int wi = blockIdx.x; wi < nw; wi += gridDim.x) {
-        const int i = rb_locate(rb_tile_off(d), m, wi);
-        const int r = __ldcg(rb_rep(d) + i);
-        const int4 tl = d.tiles[d.rep[r].tile_begin + wi - __ldcg(rb_tile_off(d) + i)];
+    const int per = (nw + gridDim.x - 1) / gridDim.x;
+    const int w_end = min(nw, ((int)blockIdx.x + 1) * per);
+    int wi = blockIdx.x * per;
+    int i = wi < w_end ? rb_locate(rb_tile_off(d), m, wi) - 1 : 0;
+    int next = wi, shift = 0;   // where replica i's run ends; tile index - work index inside it
+    for (; wi < w_end; ++wi) {
+        while (wi >= next) {
+            ++i;
+            next = __ldcg(rb_tile_off(d) + i + 1);
+            shift = d.rep[__ldcg(rb_rep(d) + i)].tile_begin - __ldcg(rb_tile_off(d) + i);
+        }
+        const int4 tl = d.tiles[wi + shift];
         const RepDev& R = tile_rep(d, tl.x);
         const int s = tl.y + threadIdx.x;
         if ((int)threadIdx.x >= tl.z) continue;
