@@ -74,6 +74,9 @@ struct mdgb_engine {
     cudaEvent_t fork_ev = nullptr;
     cudaEvent_t join_ev[3] = {nullptr, nullptr, nullptr};
     int num_sms = 0;
+    // the GPU reads the caller's pageable arrays itself (Grace: address
+    // translation through the host's page tables), so uploads skip the copy
+    bool host_direct = false;
     int pre_blocks_per_sm = 0;
     int force_blocks_per_sm[4] = {0, 0, 0, 0};
     LJ pot[MAX_TYPES][MAX_TYPES];
@@ -1246,20 +1249,33 @@ int upload_impl(mdgb_engine* e, int nrep, const int64_t* offsets, const uint16_t
     CU(cudaMemsetAsync(d.bar, 0, 8 * sizeof(unsigned int), e->stream));
     CU(cudaMemsetAsync(d.rb, 0, (4 + 3 * (size_t)nrep) * sizeof(int), e->stream));
     CU(cudaMemcpyAsync(d.rep, e->rep_host.data(), nrep * sizeof(RepDev), cudaMemcpyHostToDevice, e->stream));
-    // the caller's arrays, straight to the device staging
-    double* dpos = e->d_out;
-    double* dvel = e->d_out + 3 * (size_t)N;
-    CU(cudaMemcpyAsync(dpos, pos, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
-    if (vel) CU(cudaMemcpyAsync(dvel, vel, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
-    CU(cudaMemcpyAsync(e->d_in_t, type, (size_t)N * sizeof(uint16_t), cudaMemcpyHostToDevice, e->stream));
-    if (ntypes > 1)
-        CU(cudaMemcpyAsync(e->d_in_i, rank.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, e->stream));
-    const double* vptr = vel ? dvel : nullptr;
-    const uint16_t* tptr = e->d_in_t;
-    const int* rptr = ntypes > 1 ? e->d_in_i : nullptr;
+    // the caller's arrays: read by the scatter kernel where they lie (the
+    // GPU reaches pageable host memory), else copied to the device staging
+    // first.  Either way they are done with before this call returns (the
+    // list rebuild below synchronises).
+    const double* dpos = pos;
+    const double* vptr = vel;
+    const uint16_t* tptr = type;
+    const int* rptr = ntypes > 1 ? rank.data() : nullptr;
+    if (!e->host_direct) {
+        double* spos = e->d_out;
+        double* svel = e->d_out + 3 * (size_t)N;
+        CU(cudaMemcpyAsync(spos, pos, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        if (vel) CU(cudaMemcpyAsync(svel, vel, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        CU(cudaMemcpyAsync(e->d_in_t, type, (size_t)N * sizeof(uint16_t), cudaMemcpyHostToDevice, e->stream));
+        if (ntypes > 1)
+            CU(cudaMemcpyAsync(e->d_in_i, rank.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+        dpos = spos;
+        vptr = vel ? svel : nullptr;
+        tptr = e->d_in_t;
+        rptr = ntypes > 1 ? e->d_in_i : nullptr;
+    }
     int nt = ntypes;
     void* args[] = {(void*)&e->dev, (void*)&dpos, (void*)&vptr, (void*)&tptr, (void*)&rptr, (void*)&nt};
     CU(cudaLaunchKernel((const void*)k_scatter_in, dim3((N + 255) / 256), dim3(256), args, 0, e->stream));
+    // the kernel may read the caller's arrays and the local rank table: done
+    // before anything below can return
+    if (e->host_direct && ntypes > 1) CU(cudaStreamSynchronize(e->stream));
     e->thermo_on = e->baro_on = e->thermo_nh = false;
     if (ntypes == 1) {   // the type ids were checked on the device
         int flags = 0;
@@ -1443,6 +1459,12 @@ MDGB_API int mdgb_create(const mdgb_config* cfg, mdgb_engine** out) {
     cudaGetDeviceProperties(&prop, c.device);
     if (!prop.cooperativeLaunch) { delete e; return MDGB_ERR_UNSUPPORTED; }
     e->num_sms = prop.multiProcessorCount;
+    {
+        int pageable = 0, host_tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c.device);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, c.device);
+        e->host_direct = pageable == 1 && host_tables == 1;
+    }
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) { delete e; return MDGB_ERR_CUDA; }
     for (int c = 0; c < mdgb_engine::NCLASS; ++c)
         if (cudaStreamCreateWithFlags(&e->aux[c], cudaStreamNonBlocking) != cudaSuccess ||
