@@ -20,8 +20,11 @@
 //   orig  int      index of the atom in the caller's flat array
 //   rank  int      reference order: type-major index (particles[t][k])
 //   nn    int      neighbour count;  nbr uint32 [cap][N] (tpa-interleaved)
+//   lmask uint32   [27][N] the paired list build's hit words (rebuild scratch)
 // A neighbour entry is (j | code << 27): j the sorted index, code in 0..26
 // the periodic cell shift (dx,dy,dz in -1..1) used by the mixed path.
+// Per cell: count, start, the tagged starts of its 27 neighbour cells (nbs);
+// per rebuild: the work list of rebuilding replicas (rb).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
