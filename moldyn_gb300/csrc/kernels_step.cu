@@ -1473,10 +1473,13 @@ __global__ void __launch_bounds__(TILE, 6) k_pre(Dev d, StepParams sp) {
         for (int t = 0; t <= d.last_type; ++t)
             if (nh_psi_of_type(d, sp, t)) return;
         if (d.mixed) phase_drift<true>(d, sp, true); else phase_drift<false>(d, sp, true);
-    } else {
+        if (grid_barrier(d)) return;
+    } else if (sp.do_drift || !sp.force_rebuild) {
+        // (a forced rebuild without a step -- upload, refresh -- recomputes
+        // every mirror in its gather: nothing here to do for it)
         if (d.mixed) phase_drift<true>(d, sp, false); else phase_drift<false>(d, sp, false);
+        if (grid_barrier(d)) return;
     }
-    if (grid_barrier(d)) return;
     clk.mark(TR_DRIFT);
     phase_decide(d, sp);
     if (grid_barrier(d)) return;
