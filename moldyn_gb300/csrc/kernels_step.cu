@@ -1145,14 +1145,8 @@ __device__ void phase_scatter(const Dev& d, bool carry_forces) {
     }
 }
 
-// Canonical order inside each cell (ascending caller index), and every atom
-// moved from the scratch copy to its final slot.  One warp per cell: an
-// element's rank is the number of smaller keys (keys are distinct caller
-// indices), found by shuffling the cell's keys across the warp; the warp then
-// gathers the cell's atoms to cell_start + rank.  Cells of brute-mode
-// replicas are already in canonical (identity) order.
-// carry_forces: also move frc/epot/evir (a refresh that no force evaluation
-// follows).
+// Cells of up to 32 * SORT_MAX_PER_LANE atoms are ranked by shuffles; more
+// crowded ones by a serial insertion sort.
 constexpr int SORT_MAX_PER_LANE = 4;
 
 // The geometry of one replica that the gather needs, read through L2 (the
@@ -1180,34 +1174,133 @@ __device__ __forceinline__ void load_geom(const Dev& d, int r, CellGeom& g) {
     g.r = r;
 }
 
-// Scratch element i (the atom's index before the rebuild) to slot s of cell c.
-template <bool FM>
-__device__ __forceinline__ void gather_one(const Dev& d, const CellGeom& g, int c, int i, int s,
-                                           bool carry_forces) {
+// Scratch element i (the atom's index before the rebuild) to slot s of cell
+// c: its scratch row loaded (gather_load), then written to the slot with a
+// fresh mirror (gather_store).
+struct GatherIn {
+    double4_32a p;
+    double v[3];
+    int orig, rank;
+};
+
+__device__ __forceinline__ void gather_load(const Dev& d, int i, GatherIn& in) {
     const int N = d.ntot;
-    if (i < g.begin || i >= g.begin + g.n || s < g.begin || s >= g.begin + g.n) {
-        atomicOr(d.err, E_BOUNDS);
-        return;
-    }
-    const double4_32a p = ldcg4(d.tmp_pos + i);
-    d.pos[s] = p;
-    for (int k = 0; k < 3; ++k) d.vel[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)k * N + i);
+    in.p = ldcg4(d.tmp_pos + i);
+    for (int k = 0; k < 3; ++k) in.v[k] = __ldcg(d.tmp_d + (size_t)k * N + i);
+    in.orig = __ldcg(d.tmp_i + i);
+    in.rank = __ldcg(d.tmp_i + (size_t)N + i);
+}
+
+template <bool FM>
+__device__ __forceinline__ void gather_store(const Dev& d, const CellGeom& g, int c, int i, int s,
+                                             const GatherIn& in, bool carry_forces) {
+    const int N = d.ntot;
+    d.pos[s] = in.p;
+    for (int k = 0; k < 3; ++k) d.vel[(size_t)k * N + s] = in.v[k];
     if (carry_forces) {
         for (int k = 0; k < 3; ++k) d.frc[(size_t)k * N + s] = __ldcg(d.tmp_d + (size_t)(3 + k) * N + i);
         d.epot[s] = __ldcg(d.tmp_d + (size_t)6 * N + i);
         d.evir[s] = __ldcg(d.tmp_d + (size_t)7 * N + i);
     }
-    d.orig[s] = __ldcg(d.tmp_i + i);
-    const int rk = __ldcg(d.tmp_i + (size_t)N + i);
-    d.rank[s] = rk;
+    d.orig[s] = in.orig;
+    d.rank[s] = in.rank;
     d.cell[s] = c;
-    const float4 m = mirror_of(p, c - g.cell_base, g, g.hL, FM);
+    const float4 m = mirror_of(in.p, c - g.cell_base, g, g.hL, FM);
     d.mir[s] = m;
     d.mir0[s] = m;
-    if (rk >= 0 && rk < N) d.slot_of_rank[rk] = s;
+    if (in.rank >= 0 && in.rank < N) d.slot_of_rank[in.rank] = s;
     else atomicOr(d.err, E_BOUNDS);
 }
 
+__device__ __forceinline__ bool gather_ok(const Dev& d, const CellGeom& g, int i, int s) {
+    if (i < g.begin || i >= g.begin + g.n || s < g.begin || s >= g.begin + g.n) {
+        atomicOr(d.err, E_BOUNDS);
+        return false;
+    }
+    return true;
+}
+
+template <bool FM>
+__device__ __forceinline__ void gather_one(const Dev& d, const CellGeom& g, int c, int i, int s,
+                                           bool carry_forces) {
+    if (!gather_ok(d, g, i, s)) return;
+    GatherIn in;
+    gather_load(d, i, in);
+    gather_store<FM>(d, g, c, i, s, in, carry_forces);
+}
+
+// One cell: canonical order (ascending caller index) and the gather.
+template <bool FM>
+__device__ void sort_gather_cell(const Dev& d, const CellGeom& g, int c, int b, int n, bool carry_forces) {
+    const int N = d.ntot;
+    const int lane = threadIdx.x & 31;
+    if (g.mode == MODE_BRUTE) {
+        // the scatter kept the replica's order: slot i holds element i
+        for (int k = lane; k < n; k += 32) gather_one<FM>(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
+    } else if (n <= 32 * SORT_MAX_PER_LANE) {
+        int e[SORT_MAX_PER_LANE], key[SORT_MAX_PER_LANE], rank[SORT_MAX_PER_LANE];
+#pragma unroll
+        for (int q = 0; q < SORT_MAX_PER_LANE; ++q) {
+            const int i = q * 32 + lane;
+            e[q] = i < n ? __ldcg(d.perm + b + i) : -1;
+            const bool ok = e[q] >= 0 && e[q] < N;
+            if (i < n && !ok) atomicOr(d.err, E_BOUNDS);
+            key[q] = ok ? __ldcg(d.tmp_i + e[q]) : 0x7FFFFFFF;
+            rank[q] = 0;
+        }
+        if (n <= 32) {
+            // one key a lane, n shuffles
+            for (int k = 0; k < n; ++k) rank[0] += (__shfl_sync(0xffffffffu, key[0], k) < key[0]) ? 1 : 0;
+        } else {
+#pragma unroll
+            for (int q2 = 0; q2 < SORT_MAX_PER_LANE; ++q2) {
+                if (q2 * 32 >= n) break;
+                for (int k = 0; k < 32; ++k) {
+                    const int kk = __shfl_sync(0xffffffffu, key[q2], k);
+#pragma unroll
+                    for (int q = 0; q < SORT_MAX_PER_LANE; ++q) rank[q] += (kk < key[q]) ? 1 : 0;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < SORT_MAX_PER_LANE; ++q) {
+            const int i = q * 32 + lane;
+            if (i < n && e[q] >= 0 && e[q] < N && rank[q] < n) gather_one<FM>(d, g, c, e[q], b + rank[q], carry_forces);
+        }
+    } else {
+        // very crowded cell: serial insertion sort of the slots, then the gather
+        if (lane == 0) {
+            for (int a = 1; a < n; ++a) {
+                const int e0 = __ldcg(d.perm + b + a);
+                if (e0 < 0 || e0 >= N) { atomicOr(d.err, E_BOUNDS); break; }
+                const int k0 = __ldcg(d.tmp_i + e0);
+                int k = a - 1;
+                while (k >= 0) {
+                    const int f = __ldcg(d.perm + b + k);
+                    if (f < 0 || f >= N || __ldcg(d.tmp_i + f) <= k0) break;
+                    d.perm[b + k + 1] = f;
+                    --k;
+                }
+                d.perm[b + k + 1] = e0;
+            }
+        }
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) gather_one<FM>(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
+    }
+}
+
+// Canonical order inside each cell (ascending caller index), and every atom
+// moved from the scratch copy to its final slot.  One warp per cell: an
+// element's rank is the number of smaller keys (keys are distinct caller
+// indices), found by shuffling the cell's keys across the warp; the warp then
+// gathers the cell's atoms to cell_start + rank.  A warp takes two
+// neighbouring cells (work items 2w, 2w + 1) at a time: when both are in the
+// same cell-mode replica and hold at most 32 atoms, their loads, ranks and
+// gathers interleave, so twice the memory requests are in flight (the phase
+// is latency-bound); otherwise the cells go one after the other.  Cells of
+// brute-mode replicas are already in canonical (identity) order.
+// carry_forces: also move frc/epot/evir (a refresh that no force evaluation
+// follows).
 template <bool FM>
 __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
     const int N = d.ntot;
@@ -1217,66 +1310,56 @@ __device__ void phase_sort_gather(const Dev& d, bool carry_forces) {
     CellGeom g;
     g.r = -1;
     const int m = __ldcg(d.rb), nwork = __ldcg(rb_cell_off(d) + m);
-    for (int wi = gw; wi < nwork; wi += nw) {
-        const int i = rb_locate(rb_cell_off(d), m, wi);
+    for (int wp = gw; 2 * wp < nwork; wp += nw) {
+        const int w0 = 2 * wp;
+        const int i = rb_locate(rb_cell_off(d), m, w0);
         const int r = __ldcg(rb_rep(d) + i);
-        const int c = __ldcg(&d.rep[r].cell_base) + wi - __ldcg(rb_cell_off(d) + i);
-        const int b = __ldcg(d.cell_start + c), n = __ldcg(d.cell_count + c);
-        if (n <= 0) continue;
-        if (b < 0 || b + n > N) { if (lane == 0) atomicOr(d.err, E_CELLS); continue; }
+        const int off0 = __ldcg(rb_cell_off(d) + i), off1 = __ldcg(rb_cell_off(d) + i + 1);
+        const int c0 = __ldcg(&d.rep[r].cell_base) + w0 - off0;
+        const bool two = w0 + 1 < off1;   // the second cell is in the same replica
+        const int b0 = __ldcg(d.cell_start + c0), n0 = __ldcg(d.cell_count + c0);
+        const int b1 = two ? __ldcg(d.cell_start + c0 + 1) : 0, n1 = two ? __ldcg(d.cell_count + c0 + 1) : 0;
         if (r != g.r) load_geom(d, r, g);
-        if (g.mode == MODE_BRUTE) {
-            // the scatter kept the replica's order: slot i holds element i
-            for (int k = lane; k < n; k += 32) gather_one<FM>(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
-        } else if (n <= 32 * SORT_MAX_PER_LANE) {
-            int e[SORT_MAX_PER_LANE], key[SORT_MAX_PER_LANE], rank[SORT_MAX_PER_LANE];
-#pragma unroll
-            for (int q = 0; q < SORT_MAX_PER_LANE; ++q) {
-                const int i = q * 32 + lane;
-                e[q] = i < n ? __ldcg(d.perm + b + i) : -1;
-                const bool ok = e[q] >= 0 && e[q] < N;
-                if (i < n && !ok) atomicOr(d.err, E_BOUNDS);
-                key[q] = ok ? __ldcg(d.tmp_i + e[q]) : 0x7FFFFFFF;
-                rank[q] = 0;
+        const bool in0 = b0 >= 0 && b0 + n0 <= N, in1 = b1 >= 0 && b1 + n1 <= N;
+        if (two && g.mode == MODE_CELLS && n0 <= 32 && n1 <= 32 && in0 && in1) {
+            const int e0 = lane < n0 ? __ldcg(d.perm + b0 + lane) : -1;
+            const int e1 = lane < n1 ? __ldcg(d.perm + b1 + lane) : -1;
+            const bool ok0 = e0 >= 0 && e0 < N, ok1 = e1 >= 0 && e1 < N;
+            if ((lane < n0 && !ok0) || (lane < n1 && !ok1)) atomicOr(d.err, E_BOUNDS);
+            const int key0 = ok0 ? __ldcg(d.tmp_i + e0) : 0x7FFFFFFF;
+            const int key1 = ok1 ? __ldcg(d.tmp_i + e1) : 0x7FFFFFFF;
+            int rank0 = 0, rank1 = 0;
+            const int nm = max(n0, n1);
+            for (int k = 0; k < nm; ++k) {
+                rank0 += (__shfl_sync(0xffffffffu, key0, k) < key0) ? 1 : 0;
+                rank1 += (__shfl_sync(0xffffffffu, key1, k) < key1) ? 1 : 0;
             }
-            if (n <= 32) {
-                // the common case: one key a lane, n shuffles
-                for (int k = 0; k < n; ++k) rank[0] += (__shfl_sync(0xffffffffu, key[0], k) < key[0]) ? 1 : 0;
-            } else {
-#pragma unroll
-                for (int q2 = 0; q2 < SORT_MAX_PER_LANE; ++q2) {
-                    if (q2 * 32 >= n) break;
-                    for (int k = 0; k < 32; ++k) {
-                        const int kk = __shfl_sync(0xffffffffu, key[q2], k);
-#pragma unroll
-                        for (int q = 0; q < SORT_MAX_PER_LANE; ++q) rank[q] += (kk < key[q]) ? 1 : 0;
-                    }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < SORT_MAX_PER_LANE; ++q) {
-                const int i = q * 32 + lane;
-                if (i < n && e[q] >= 0 && e[q] < N && rank[q] < n) gather_one<FM>(d, g, c, e[q], b + rank[q], carry_forces);
-            }
-        } else {
-            // very crowded cell: serial insertion sort of the slots, then the gather
-            if (lane == 0) {
-                for (int a = 1; a < n; ++a) {
-                    const int e0 = __ldcg(d.perm + b + a);
-                    if (e0 < 0 || e0 >= N) { atomicOr(d.err, E_BOUNDS); break; }
-                    const int k0 = __ldcg(d.tmp_i + e0);
-                    int k = a - 1;
-                    while (k >= 0) {
-                        const int f = __ldcg(d.perm + b + k);
-                        if (f < 0 || f >= N || __ldcg(d.tmp_i + f) <= k0) break;
-                        d.perm[b + k + 1] = f;
-                        --k;
-                    }
-                    d.perm[b + k + 1] = e0;
-                }
-            }
-            __syncwarp();
-            for (int k = lane; k < n; k += 32) gather_one<FM>(d, g, c, __ldcg(d.perm + b + k), b + k, carry_forces);
+            const bool go0 = ok0 && rank0 < n0 && gather_ok(d, g, e0, b0 + rank0);
+            const bool go1 = ok1 && rank1 < n1 && gather_ok(d, g, e1, b1 + rank1);
+            GatherIn g0, g1;
+            if (go0) gather_load(d, e0, g0);
+            if (go1) gather_load(d, e1, g1);
+            if (go0) gather_store<FM>(d, g, c0, e0, b0 + rank0, g0, carry_forces);
+            if (go1) gather_store<FM>(d, g, c0 + 1, e1, b1 + rank1, g1, carry_forces);
+            continue;
+        }
+        if (n0 > 0) {
+            if (in0) sort_gather_cell<FM>(d, g, c0, b0, n0, carry_forces);
+            else if (lane == 0) atomicOr(d.err, E_CELLS);
+        }
+        if (w0 + 1 >= nwork) continue;
+        // the second cell on its own (it may begin the next replica)
+        int r1 = r, c1 = c0 + 1, bb = b1, nn = n1;
+        if (!two) {
+            r1 = __ldcg(rb_rep(d) + i + 1);
+            c1 = __ldcg(&d.rep[r1].cell_base);
+            bb = __ldcg(d.cell_start + c1);
+            nn = __ldcg(d.cell_count + c1);
+            if (r1 != g.r) load_geom(d, r1, g);
+        }
+        if (nn > 0) {
+            if (bb >= 0 && bb + nn <= N) sort_gather_cell<FM>(d, g, c1, bb, nn, carry_forces);
+            else if (lane == 0) atomicOr(d.err, E_CELLS);
         }
     }
 }
