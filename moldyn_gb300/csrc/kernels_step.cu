@@ -1107,41 +1107,73 @@ __device__ void phase_scan_c(const Dev& d, int chunk) {
 
 // carry_forces: also move frc/epot/evir (a refresh that no force evaluation
 // follows); a step's force pass rewrites them after the rebuild anyway.
-__device__ void phase_scatter(const Dev& d, bool carry_forces) {
+// One atom's move to the scratch copy: its inputs (ScatterIn, loaded for two
+// tiles before either is stored, so a thread has both in flight) and its
+// slot, perm[slot] = s.
+struct ScatterIn {
+    double4_32a p;
+    double v[3];
+    int cell, slot, orig, rank;
+};
+
+__device__ __forceinline__ void scatter_load(const Dev& d, const RepDev& R, int s, ScatterIn& in) {
     const int N = d.ntot;
+    in.cell = d.tmp_i[2 * (size_t)N + s];
+    const int within = d.tmp_i[3 * (size_t)N + s];
+    in.p = d.pos[s];
+    for (int k = 0; k < 3; ++k) in.v[k] = d.vel[(size_t)k * N + s];
+    in.orig = d.orig[s];
+    in.rank = d.rank[s];
+    // brute mode: one cell holds the whole replica in its current order
+    const bool cell_ok = in.cell >= R.cell_base && in.cell < R.cell_base + R.cell_cap;
+    in.slot = R.mode == MODE_BRUTE ? s : (cell_ok ? __ldcg(d.cell_start + in.cell) + within : -1);
+    if (!cell_ok) in.cell = -1;
+}
+
+__device__ __forceinline__ void scatter_store(const Dev& d, const RepDev& R, int s, const ScatterIn& in,
+                                              bool carry_forces) {
+    const int N = d.ntot;
+    if (in.cell < 0 || in.slot < R.begin || in.slot >= R.begin + R.n) { atomicOr(d.err, E_CELLS); return; }
+    d.perm[in.slot] = s;
+    d.tmp_pos[s] = in.p;
+    for (int k = 0; k < 3; ++k) d.tmp_d[(size_t)k * N + s] = in.v[k];
+    if (carry_forces) {
+        for (int k = 0; k < 3; ++k) d.tmp_d[(size_t)(3 + k) * N + s] = d.frc[(size_t)k * N + s];
+        d.tmp_d[(size_t)6 * N + s] = d.epot[s];
+        d.tmp_d[(size_t)7 * N + s] = d.evir[s];
+    }
+    d.tmp_i[s] = in.orig;
+    d.tmp_i[(size_t)N + s] = in.rank;
+}
+
+__device__ void phase_scatter(const Dev& d, bool carry_forces) {
     // a contiguous run of the rebuilding replicas' tiles per block (the
-    // replica record is fetched only when the run crosses into the next)
+    // replica record is fetched only when the run crosses into the next);
+    // two tiles of a replica at a time
     const int m = __ldcg(d.rb), nw = __ldcg(rb_tile_off(d) + m);
     const int per = (nw + gridDim.x - 1) / gridDim.x;
     const int w_end = min(nw, ((int)blockIdx.x + 1) * per);
     int wi = blockIdx.x * per;
     int i = wi < w_end ? rb_locate(rb_tile_off(d), m, wi) - 1 : 0;
     int next = wi, shift = 0;   // where replica i's run ends; tile index - work index inside it
-    for (; wi < w_end; ++wi) {
+    while (wi < w_end) {
         while (wi >= next) {
             ++i;
             next = __ldcg(rb_tile_off(d) + i + 1);
             shift = d.rep[__ldcg(rb_rep(d) + i)].tile_begin - __ldcg(rb_tile_off(d) + i);
         }
-        const int4 tl = d.tiles[wi + shift];
-        const RepDev& R = tile_rep(d, tl.x);
-        const int s = tl.y + threadIdx.x;
-        if ((int)threadIdx.x >= tl.z) continue;
-        const int cell = d.tmp_i[2 * (size_t)N + s];
-        if (cell < R.cell_base || cell >= R.cell_base + R.cell_cap) { atomicOr(d.err, E_CELLS); continue; }
-        // brute mode: one cell holds the whole replica in its current order
-        const int slot = R.mode == MODE_BRUTE ? s : __ldcg(d.cell_start + cell) + d.tmp_i[3 * (size_t)N + s];
-        if (slot < R.begin || slot >= R.begin + R.n) { atomicOr(d.err, E_CELLS); continue; }
-        d.perm[slot] = s;
-        d.tmp_pos[s] = d.pos[s];
-        for (int k = 0; k < 3; ++k) d.tmp_d[(size_t)k * N + s] = d.vel[(size_t)k * N + s];
-        if (carry_forces) {
-            for (int k = 0; k < 3; ++k) d.tmp_d[(size_t)(3 + k) * N + s] = d.frc[(size_t)k * N + s];
-            d.tmp_d[(size_t)6 * N + s] = d.epot[s];
-            d.tmp_d[(size_t)7 * N + s] = d.evir[s];
-        }
-        d.tmp_i[s] = d.orig[s];
-        d.tmp_i[(size_t)N + s] = d.rank[s];
+        const bool two = wi + 1 < w_end && wi + 1 < next;
+        const int4 ta = d.tiles[wi + shift];
+        const int4 tb = two ? d.tiles[wi + 1 + shift] : make_int4(0, 0, 0, 0);
+        const RepDev& R = tile_rep(d, ta.x);
+        const int sa = ta.y + threadIdx.x, sb = tb.y + threadIdx.x;
+        const bool aa = (int)threadIdx.x < ta.z, ab = two && (int)threadIdx.x < tb.z;
+        ScatterIn xa, xb;
+        if (aa) scatter_load(d, R, sa, xa);
+        if (ab) scatter_load(d, R, sb, xb);
+        if (aa) scatter_store(d, R, sa, xa, carry_forces);
+        if (ab) scatter_store(d, R, sb, xb, carry_forces);
+        wi += two ? 2 : 1;
     }
 }
 
