@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(LM_WARPS * 32, 10) k_list_masks(Dev d) {
         const int nc[3] = {W->nc[0], W->nc[1], W->nc[2]};
         const int base = W->cell_base;
         const int local = c - base;
-        if (local >= nc[0] * nc[1] * nc[2]) continue;   // spare cell capacity
+        if (local >= nc[0] * nc[1] * nc[2]) continue;   // a guard: the work list holds the grid only
         const long long rbeg = W->begin;
         const int rn = W->n;
         const int ib = d.cell_start[c], in = d.cell_count[c];
@@ -299,7 +299,7 @@ __device__ __forceinline__ void list_direct(const Dev& d, uint32_t* lb_smem, boo
         const int nc[3] = {W->nc[0], W->nc[1], W->nc[2]};
         const int base = W->cell_base;
         const int local = c - base;
-        if (local >= nc[0] * nc[1] * nc[2]) continue;   // spare cell capacity
+        if (local >= nc[0] * nc[1] * nc[2]) continue;   // a guard: the work list holds the grid only
         const long long rbeg = W->begin;
         const int rn = W->n, tpa = W->tpa;
         const int ib = d.cell_start[c], in = d.cell_count[c];
